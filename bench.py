@@ -1,0 +1,284 @@
+"""Benchmark of the grid-erosion step on GB300.
+
+Workload (the metric's configuration): a 4096 x 4096 FP32 world, 6-octave
+simplex fBm heightmap (base frequency 1/128, lacunarity 2, gain 0.5, seed 0)
+scaled to [0, 64]; dt 0.02, G 9.81, Kc 0.1, Ks = Kd = 0.05, Ke 0.015;
+thermal erosion with talus tan 0.65 and slippage 0.3; Bernoulli rain of 0.5
+with p = 0.001 per cell and step from Philox4x32-10.  Data are synthetic
+(seeded noise).  One bench "step" is one erosion step of the whole grid; the
+metric is cell-steps per second.  The 9 carried fields (604 MB) exceed the
+129 MB L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is the fused kernel with fields resident in
+HBM; `plain_value` the per-pass kernels; `e2e` goes through the C ABI with
+pinned host buffers (upload of the initial fields and download of the
+result inside the timed region).  `--impl reference` times the CPU
+restatement of the reference's passes (the reference itself is GLSL/OpenGL
+and cannot run without a graphics stack).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "hydro-gen_gb300"))
+
+N_GRID = 4096
+BYTES_PER_CELL_STEP = 72  # 9 FP32 fields (rock, water, sediment, 4 fluxes, u, v) read + written
+METRIC = "cell-steps/s fused vs per-pass at 4096²"
+UNIT = "cell-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_GRID)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic_per_cell_step():
+    """DRAM bytes per cell-step of the fused kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "fused_step_config2.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_cell_step:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.p is None:
+            return
+        time.sleep(0.15)
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline(n_sample=1024, budget_s=12.0):
+    """The float oracle (CPU restatement of the reference passes), all host
+    threads, on an n_sample^2 world with the same physics and rain."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    w = O.OracleWorld(n_sample, 32)
+    w.set("rock", O.fbm(n_sample))
+    s, o = O.workload("config2")
+    w.step(s, o, 1)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        w.step(s, o, 1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s and steps >= 3:
+            break
+    return {"value": steps * n_sample * n_sample / el, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"{n_sample}x{n_sample} world, same physics and rain, {steps} steps in {el:.1f} s "
+                      f"(float oracle, OpenMP over rows)"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    n = 1024
+    w = O.OracleWorld(n, 32)
+    w.set("rock", O.fbm(n))
+    s, o = O.workload("config2")
+    w.step(s, o, args.warmup)
+    t0 = time.perf_counter()
+    w.step(s, o, args.steps)
+    el = time.perf_counter() - t0
+    v = args.steps * n * n / el
+    sample = (f"each step is one erosion step of a {n}x{n} world with the {N_GRID}^2 workload's physics, rain "
+              f"and noise statistics (float CPU restatement of the GLSL passes; the reference's GL path needs a "
+              f"graphics stack, unavailable on this box)")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"config2 erosion {N_GRID}x{N_GRID}", "sample_grid": n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world_size, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import torch
+    import hydrogen as H
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    n = args.n
+    cells = n * n
+    w = H.World(n)
+    w.init_heightmap(H.noise(seed=0))
+    H.configure(w, "config2")
+    w.set_options(H.options(H.RAIN_BERNOULLI, p=0.001, seed=0, terrain_id=rank))
+    init = {f: w.download(f) for f in ("rock",)}
+    stream = torch.cuda.ExternalStream(w.stream)
+
+    def timed(mode, steps, warmup):
+        w.step(warmup, mode)
+        w.sync()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = H.lib.hg_launch_count()
+        e0.record(stream)
+        w.step(steps, mode)
+        e1.record(stream)
+        e1.synchronize()
+        launches = H.lib.hg_launch_count() - l0
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, launches
+
+    # per-pass kernels (denominator of the fused-vs-plain ratio)
+    plain_steps = min(args.steps, 100)
+    plain_ms, _ = timed(H.MODE_PLAIN, plain_steps, max(3, args.warmup // 4))
+    # fused kernel: the headline
+    w.upload("rock", init["rock"])
+    for f in ("water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b"):
+        w.upload(f, init["rock"] * 0)
+    w.step_count = 0
+    with Clocks(local) as clk:
+        fused_ms, launches = timed(H.MODE_FUSED, args.steps, args.warmup)
+    fused_per_launch_ms = fused_ms / launches if launches else None
+
+    value = world_size * cells * args.steps / (fused_ms / 1e3)
+    plain_value = world_size * cells * plain_steps / (plain_ms / 1e3)
+
+    # e2e: C ABI with pinned host buffers, copies inside the timed region
+    host = {f: torch.zeros((n, n), dtype=torch.float32).pin_memory() for f in H.STATE_FIELDS[:7]}
+    host["rock"].copy_(torch.from_numpy(init["rock"]))
+    outs = {f: torch.empty((n, n), dtype=torch.float32).pin_memory() for f in ("rock", "water", "sediment")}
+    barrier()
+    t0 = time.perf_counter()
+    for f, t in host.items():
+        H.check(H.lib.hg_world_upload(w.h, H.FIELDS[f], t.data_ptr()))
+    w.step_count = 0
+    w.step(args.steps, H.MODE_FUSED)
+    for f, t in outs.items():
+        H.check(H.lib.hg_world_download(w.h, H.FIELDS[f], t.data_ptr()))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = 7 * cells * 4 / args.steps
+    d2h = 3 * cells * 4 / args.steps
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_CELL_STEP * cells / (fused_per_launch_ms / 1e3) / 1e9
+    tpc = profiled_traffic_per_cell_step()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": fused_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded simplex fBm terrain, Philox rain)",
+        "config": {"workload": f"config2 erosion {n}x{n} FP32, thermal on, Bernoulli rain p=0.001",
+                   "grid": n, "parallelism": f"replicas x{world_size}" if world_size > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (9 fields x 4 B x n^2)"},
+        "plain_value": plain_value, "fused_vs_plain": value / plain_value,
+        "plain_ms_per_step": plain_ms / plain_steps,
+        "pct_hbm_peak": 100.0 * achieved / peak,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": tpc * cells if tpc else None,
+                     "algorithmic_bytes_per_launch": BYTES_PER_CELL_STEP * cells},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "e2e": {"value": world_size * cells * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,312 @@
+// Per-cell arithmetic of the grid-erosion step, shared by every kernel.
+//
+// Each function is the body of one GLSL pass for ONE cell, with the
+// neighbourhood passed in as values, so the per-pass kernels, the fused
+// kernel and the fused kernel's out-of-tile fallback evaluate exactly the same
+// float expression tree (one rounding per operation; the library is built
+// with -fmad=false so nvcc does not contract a*b+c).  Each function cites the
+// GLSL lines it implements (paths inside the hydro-gen project).
+//
+// The world is the single-material form of the reference model: rock in
+// heightmap.r, an empty dirt layer (heightmap.g == 0, sedimap.g == 0,
+// Kconv == 0, Kspeed[1] == 0), which the reference evaluates with the dirt
+// terms vanishing exactly; the comments below say where that is used.
+#pragma once
+#include <cstdint>
+
+namespace hg {
+
+// GLSL built-ins with GLSL's operand order (min(x,y) = y<x?y:x, ...).
+__device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; }
+__device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+__device__ __forceinline__ float gmix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+
+// out-of-range height used by the flux and thermal passes
+// (glsl/hydro_flux.glsl:36, glsl/thermal_erosion.glsl:23): 999999999999.0 as float
+constexpr float FAR_HEIGHT = 999999995904.0f;
+
+// Single-precision arctangent (csrc/fit_atan.py): three branches keep the
+// polynomial argument within |u| <= tan(pi/8),
+//   x <= tan(pi/8): poly(x);  x <= tan(3pi/8): pi/4 + poly((x-1)/(x+1));
+//   else pi/2 - poly(1/x);    poly(u) = u + u*(s*P(s)), s = u*u.
+// Max error 2.5 ulp; monotone non-decreasing on x >= 0 (checked over every
+// positive float).
+__device__ __forceinline__ float poly_atan_core(float u) {
+    const float c0 = -3.333333135e-01f, c1 = 1.999990344e-01f, c2 = -1.428200752e-01f,
+                c3 = 1.104469076e-01f, c4 = -8.476266265e-02f, c5 = 4.744043201e-02f;
+    float s = __fmul_rn(u, u);
+    float p = c5;
+    p = __fadd_rn(__fmul_rn(p, s), c4);
+    p = __fadd_rn(__fmul_rn(p, s), c3);
+    p = __fadd_rn(__fmul_rn(p, s), c2);
+    p = __fadd_rn(__fmul_rn(p, s), c1);
+    p = __fadd_rn(__fmul_rn(p, s), c0);
+    return __fadd_rn(u, __fmul_rn(u, __fmul_rn(s, p)));
+}
+__device__ __forceinline__ float poly_atanf(float x) {
+    float ax = fabsf(x), r;
+    if (ax <= 0.414213562f) r = poly_atan_core(ax);
+    else if (ax <= 2.41421356f)
+        r = __fadd_rn(0.785398163f, poly_atan_core(__fdiv_rn(__fsub_rn(ax, 1.0f), __fadd_rn(ax, 1.0f))));
+    else r = __fsub_rn(1.57079637f, poly_atan_core(__fdiv_rn(1.0f, ax)));
+    return copysignf(r, x);
+}
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers:
+// as easy as 1, 2, 3", SC'11) ---------------------------------------------------
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+        uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+        uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// Rain settings resolved for one step.
+struct RainStep {
+    int active;          // this step rains
+    int bernoulli;       // 0 uniform, 1 Bernoulli
+    float amount;
+    uint32_t threshold;  // Bernoulli: rain when the Philox word < threshold
+    uint32_t seed_lo, seed_hi, terrain_id;
+    uint32_t step;       // 1-based step number (Philox counter word 2)
+};
+
+// One Philox call covers the four cells x0..x0+3 (x0 % 4 == 0):
+// counter (x0/4, y, step, terrain), key (seed).  Cell x uses word x % 4.
+__device__ __forceinline__ void rain_words4(const RainStep& r, int x0, int y, uint32_t out[4]) {
+    out[0] = (uint32_t)x0 >> 2; out[1] = (uint32_t)y; out[2] = r.step; out[3] = r.terrain_id;
+    philox4x32_10(out, r.seed_lo, r.seed_hi);
+}
+
+// glsl/rain.glsl:48-53 with the workload's rain amount: water += incr.
+__device__ __forceinline__ float rain_incr(const RainStep& r, uint32_t word) {
+    if (!r.bernoulli) return r.amount;
+    return word < r.threshold ? r.amount : 0.0f;
+}
+
+// ---- constants of one step -----------------------------------------------------
+struct StepConsts {
+    int n;
+    float dt, G, EK;      // d_t, G, ENERGY_KEPT
+    float Kc;
+    float Kls0, Kld0;     // d_t*Ks[0], d_t*Kd[0] (rock)
+    float Kls1, Kld1;     // d_t*Ks[1], d_t*Kd[1] (empty dirt layer)
+    float Ks0;            // Ks[0] when no per-cell field is set
+    const float* ks_field;  // per-cell Ks[0] or nullptr
+    float evap;           // 1 - Ke*d_t
+    float Kalpha0, Kspeed0;
+    int thermal;          // thermal layer-0 passes enabled (Kspeed[0] != 0)
+    float talus_x_cross;  // smallest slope whose poly_atanf exceeds Kalpha0
+    float talus_b_diag;   // smallest height drop whose diagonal slope does
+};
+
+// ---- hydro_flux, glsl/hydro_flux.glsl:77-166 -------------------------------------
+// w* are neighbour totals (rock + water after rain; FAR_HEIGHT outside the
+// grid), in* the neighbours' old flux facing this cell (left.fR, right.fL,
+// top.fB, bottom.fT; 0 outside).  The 1-layer total is rock + water: the
+// reference's (r + d2) + g with g == 0 is the same float.
+struct FluxOut { float fl, fr, ft, fb, d2, u, v, vz; };
+
+__device__ __forceinline__ FluxOut cell_flux(const StepConsts& c, int x, int y,
+                                             float w_c, float d1,
+                                             float fl, float fr, float ft, float fb,
+                                             float wl, float wr, float wt, float wb,
+                                             float inl, float inr, float int_, float inb) {
+    FluxOut o;
+    // :88-92 total height differences; :100-107 new outflow (A == L == 1, the
+    // products and quotients by 1 are exact and dropped)
+    float dhl = w_c - wl, dhr = w_c - wr, dht = w_c - wt, dhb = w_c - wb;
+    o.fl = gmax(0.0f, c.EK * fl + c.dt * (c.G * dhl));
+    o.fr = gmax(0.0f, c.EK * fr + c.dt * (c.G * dhr));
+    o.ft = gmax(0.0f, c.EK * ft + c.dt * (c.G * dht));
+    o.fb = gmax(0.0f, c.EK * fb + c.dt * (c.G * dhb));
+    // :110-119 closed boundaries
+    if (x <= 0) o.fl = 0.0f;
+    else if (x >= c.n - 1) o.fr = 0.0f;
+    if (y <= 0) o.fb = 0.0f;
+    else if (y >= c.n - 1) o.ft = 0.0f;
+    // :121-127 scale outflow to the available water
+    float sum_in = inl + inr + int_ + inb;
+    float sum_out = o.fl + o.fr + o.ft + o.fb;
+    float K = gmin(1.0f, d1 / (sum_out * c.dt));
+    o.fl *= K; o.fr *= K; o.ft *= K; o.fb *= K;
+    sum_out *= K;
+    // :133-134 water update
+    float d_volume = c.dt * (sum_in - sum_out);
+    o.d2 = gmax(0.0f, d1 + d_volume);
+    // :144-161 velocity from the OLD flux field
+    o.vz = d1 + o.d2;
+    if (o.vz > 0.0f) {
+        o.u = (inl - fl + fr - inr) / o.vz;
+        o.v = (inb - fb + ft - int_) / o.vz;
+    } else {
+        o.u = 0.0f; o.v = 0.0f;
+    }
+    return o;
+}
+
+// ---- hydro_erosion, glsl/hydro_erosion.glsl:23-92 --------------------------------
+// b* are the neighbours' rock heights (0 outside the grid: imageLoad of an
+// out-of-range texel).  With the dirt channel at 0, (r.r + r.g) - l.r - l.g
+// equals r.r - l.r exactly.
+__device__ __forceinline__ void cell_erosion(const StepConsts& c, float Kls0, float u, float v, float vz,
+                                             float& b, float& s,
+                                             float br, float bl, float bb, float bt) {
+    // :45-52 erosion speed, faded out in very shallow water
+    float len = sqrtf(u * u + v * v);
+    float ero_vel = len;
+    if (vz < 1e-3f) {
+        float dd = gmax(5e-4f, vz);
+        float t = gclamp((dd - 1e-3f) / (5e-4f - 1e-3f), 0.0f, 1.0f);
+        t = t * t * (3.0f - 2.0f * t);
+        ero_vel = gmix(len, 0.0f, t);
+    }
+    // :23-35, :56-57 terrain normal -> sin of the tilt
+    float dx = br - bl;
+    float dz = bt - bb;
+    float cx = dx * 2.0f - 0.0f * dz;
+    float cy = 0.0f * 0.0f - 2.0f * 2.0f;
+    float cz = 2.0f * dz - dx * 0.0f;
+    float len3 = sqrtf(cx * cx + cy * cy + cz * cz);
+    float ny = cy / len3;
+    float sin_a = fabsf(sqrtf(1.0f - ny * ny));
+    // :58-83 layer loop.  Dirt layer (i = 1) first: with no dirt and no dirt
+    // sediment it dissolves Kls1*c, hands all of it back and continues with
+    // cap == 0, unless Kls1*c rounds to 0, in which case the reference breaks
+    // out of the loop before the rock layer.
+    float cap = 0.0f;
+    float cc = gmax(0.0f, c.Kc * gmax(0.02f, sin_a) * ero_vel - cap);
+    if (cc > 0.0f && !(c.Kls1 * cc > 0.0f)) return;
+    // rock layer (i = 0)
+    if (cc > s) {
+        float delta = Kls0 * (cc - s);
+        b = b - delta;
+        s = s + delta;
+        if (b < 0.0f) {  // cap += old terrain is dropped: no later layer reads it
+            s = s + b;
+            b = 0.0f;
+        }
+    } else {
+        float delta = c.Kld0 * (s - cc);
+        b = b + delta;
+        s = s - delta;
+    }
+    // :84-88 conversion with Kconv == 0 leaves s unchanged
+}
+
+// ---- sediment_transport, glsl/sediment_transport.glsl:66-93 ----------------------
+// Back-trace point of the semi-Lagrangian step (:70, clamp :26-29).
+__device__ __forceinline__ void backtrace(const StepConsts& c, int x, int y, float u, float v,
+                                          float& px, float& py) {
+    float maxc = (float)(c.n - 1);
+    px = gclamp((float)x - u * c.dt, 0.0f, maxc);
+    py = gclamp((float)y - v * c.dt, 0.0f, maxc);
+}
+
+// img_bilinear, glsl/img_interpolation.glsl:3-22: s00 at (ix, iy), s10 at
+// (ix+1, iy), s01 at (ix, iy+1), s11 at (ix+1, iy+1), out-of-range taps 0.
+__device__ __forceinline__ float bilinear_mix(float px, float py, float s00, float s10, float s01, float s11) {
+    float fx = px - floorf(px), fy = py - floorf(py);
+    float v1 = gmix(s00, s10, fx);
+    float v2 = gmix(s01, s11, fx);
+    return gmix(v1, v2, fy);
+}
+
+// ---- thermal_erosion (layer 0), glsl/thermal_erosion.glsl:28-109 ------------------
+// Outflow of one cell toward its 8 neighbours, order L, R, T, B, LT, RT, LB, RB
+// (cross (-1,0),(1,0),(0,1),(0,-1); diagonal (-1,1),(1,1),(-1,-1),(1,-1)).
+// nb[k] is the neighbour's rock (FAR_HEIGHT outside the grid).  Returns the
+// mask of marked directions and S and bk such that the outflow toward a
+// marked direction k is (S * dh_k) / bk.
+struct ThermalOut { float S, bk; uint32_t mask; };
+
+// Faithful form: one arctangent per downhill direction, as in the shader.
+__device__ __forceinline__ ThermalOut cell_thermal_ref(const StepConsts& c, float b, const float nb[8]) {
+    float dh[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];  // 0 + (b - nb) == b - nb
+    float H = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (dh[k] > H) H = dh[k];
+    H = gmin(b, H);
+    ThermalOut o{0.0f, 0.0f, 0u};
+    float sharp = 1.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float bb = dh[k];
+        if (bb <= 0.0f) continue;
+        float slope = k < 4 ? bb : bb / 1.41421354f;  // d = L (cross) or L*sqrt(2)
+        float alph = poly_atanf(slope);
+        if (alph > c.Kalpha0) {
+            float newsh = 1.0f + alph - c.Kalpha0;
+            if (newsh > sharp) sharp = newsh;
+            o.bk += bb;
+            o.mask |= 1u << k;
+        }
+    }
+    sharp *= sharp * sharp;
+    o.S = c.dt * c.Kspeed0 * sharp * H / 2.0f;  // a == L == 1
+    return o;
+}
+
+// Same result with one arctangent per cell.  poly_atanf is monotone
+// non-decreasing on x >= 0 (checked over every positive float), so
+// "poly_atanf(slope) > Kalpha0" is "slope >= talus_x_cross" (diagonal:
+// "drop >= talus_b_diag", division rounding being monotone too), and the
+// largest marked sharpness is that of the steepest marked slope.
+__device__ __forceinline__ ThermalOut cell_thermal_fast(const StepConsts& c, float b, const float nb[8]) {
+    float dh[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];
+    float H = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (dh[k] > H) H = dh[k];
+    H = gmin(b, H);
+    ThermalOut o{0.0f, 0.0f, 0u};
+    float max_cross = 0.0f, max_diag = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        float bb = dh[k];
+        bool marked = k < 4 ? (bb >= c.talus_x_cross) : (bb >= c.talus_b_diag);
+        if (bb > 0.0f && marked) {
+            o.bk += bb;
+            o.mask |= 1u << k;
+            if (k < 4) max_cross = fmaxf(max_cross, bb);
+            else max_diag = fmaxf(max_diag, bb);
+        }
+    }
+    float sharp = 1.0f;
+    if (o.mask) {
+        float slope = fmaxf(max_cross, max_diag / 1.41421354f);
+        float alph = poly_atanf(slope);
+        float newsh = 1.0f + alph - c.Kalpha0;
+        if (newsh > sharp) sharp = newsh;
+    }
+    sharp *= sharp * sharp;
+    o.S = c.dt * c.Kspeed0 * sharp * H / 2.0f;
+    return o;
+}
+
+// ---- thermal_transport (layer 0), glsl/thermal_transport.glsl:31-65 ----------------
+// own[k]: this cell's outflow in direction order L,R,T,B,LT,RT,LB,RB;
+// inflow: L.R, R.L, T.B, B.T, LT.RB, RT.LB, LB.RT, RB.LT (0 outside).
+__device__ __forceinline__ float cell_thermal_apply(float b, const float own[8], const float in[8]) {
+    float in_flux = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) in_flux += in[k];
+    float sum = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sum -= own[k];
+    sum += in_flux;
+    return b + sum;
+}
+
+}  // namespace hg

@@ -1,0 +1,294 @@
+"""Python binding of libhydrogen_gb300.so (ctypes over the C ABI in include/hydrogen.h).
+
+This mirrors the reference's erosion interface: an ErosionSettings struct
+with Erosion_data's fields and std140 layout (glsl/bindings.glsl:39-60), a
+RainSettings struct mirroring Rain_data (glsl/bindings.glsl:62-68), a World
+that owns the device fields (State::World::Textures, src/state.hpp:59-76),
+World.init_heightmap for World::gen_heightmap (src/state.cpp:116-147) and
+World.step for Erosion::dispatch_grid (src/erosion.cpp:158-200).
+
+Errors raise HydrogenError carrying the library's status code and message.
+The library must be built (build.build()); importing this module without it
+raises ImportError: there is no CPU fallback.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhydrogen_gb300.so")
+HEADER = os.path.join(HERE, "..", "include", "hydrogen.h")
+
+HG_OK = 0
+STATUS = {-1: "HG_ERR_INVALID", -2: "HG_ERR_OOM", -3: "HG_ERR_CUDA", -4: "HG_ERR_TIMEOUT",
+          -5: "HG_ERR_UNSUPPORTED", -6: "HG_ERR_IO", -7: "HG_ERR_STATE"}
+HG_AUTO = -1
+RAIN_OFF, RAIN_UNIFORM, RAIN_BERNOULLI = 0, 1, 2
+MODE_PLAIN, MODE_FUSED = 0, 1
+FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_t": 5, "flux_b": 6,
+          "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10}
+STATE_FIELDS = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"]
+
+
+class HydrogenError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class ErosionSettings(ctypes.Structure):
+    """Erosion_data, glsl/bindings.glsl:39-60 (std140, 96 bytes)."""
+    _fields_ = [("particle_count", ctypes.c_uint32), ("Kc", ctypes.c_float),
+                ("Kalpha", ctypes.c_float * 2), ("Kconv", ctypes.c_float), ("_pad0", ctypes.c_float),
+                ("Ks", ctypes.c_float * 2), ("Kd", ctypes.c_float * 2), ("Ke", ctypes.c_float),
+                ("ENERGY_KEPT", ctypes.c_float), ("Kspeed", ctypes.c_float * 2), ("G", ctypes.c_float),
+                ("d_t", ctypes.c_float), ("density", ctypes.c_float), ("init_volume", ctypes.c_float),
+                ("friction", ctypes.c_float), ("inertia", ctypes.c_float), ("min_volume", ctypes.c_float),
+                ("min_velocity", ctypes.c_float), ("ttl", ctypes.c_uint32), ("_pad1", ctypes.c_uint32)]
+
+
+class RainSettings(ctypes.Structure):
+    """Rain_data, glsl/bindings.glsl:62-68 (20 bytes)."""
+    _fields_ = [("amount", ctypes.c_float), ("mountain_thresh", ctypes.c_float),
+                ("mountain_multip", ctypes.c_float), ("period", ctypes.c_int32), ("drops", ctypes.c_float)]
+
+
+class StepOptions(ctypes.Structure):
+    _fields_ = [("rain_mode", ctypes.c_int32), ("rain_probability", ctypes.c_float),
+                ("rain_seed", ctypes.c_uint64), ("terrain_id", ctypes.c_uint32), ("thermal", ctypes.c_int32),
+                ("temporal_depth", ctypes.c_int32), ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
+
+
+class NoiseSettings(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint32), ("octaves", ctypes.c_int32), ("frequency", ctypes.c_float),
+                ("lacunarity", ctypes.c_float), ("gain", ctypes.c_float), ("out_min", ctypes.c_float),
+                ("out_max", ctypes.c_float)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with hydro-gen_gb300/build.py (no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    sig = {
+        "hg_version": (ctypes.c_char_p, []),
+        "hg_last_error": (ctypes.c_char_p, []),
+        "hg_launch_count": (ctypes.c_uint64, []),
+        "hg_default_erosion_settings": (ctypes.c_int, [ctypes.POINTER(ErosionSettings)]),
+        "hg_default_rain_settings": (ctypes.c_int, [ctypes.POINTER(RainSettings)]),
+        "hg_default_step_options": (ctypes.c_int, [ctypes.POINTER(StepOptions)]),
+        "hg_world_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(P)]),
+        "hg_world_destroy": (ctypes.c_int, [P]),
+        "hg_world_size": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
+        "hg_world_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
+        "hg_set_erosion_settings": (ctypes.c_int, [P, ctypes.POINTER(ErosionSettings)]),
+        "hg_get_erosion_settings": (ctypes.c_int, [P, ctypes.POINTER(ErosionSettings)]),
+        "hg_set_rain_settings": (ctypes.c_int, [P, ctypes.POINTER(RainSettings)]),
+        "hg_set_step_options": (ctypes.c_int, [P, ctypes.POINTER(StepOptions)]),
+        "hg_init_heightmap": (ctypes.c_int, [P, ctypes.POINTER(NoiseSettings)]),
+        "hg_init_ks_field": (ctypes.c_int, [P, ctypes.POINTER(NoiseSettings), ctypes.c_float, ctypes.c_float]),
+        "hg_clear_ks_field": (ctypes.c_int, [P]),
+        "hg_world_upload": (ctypes.c_int, [P, ctypes.c_int, P]),
+        "hg_world_download": (ctypes.c_int, [P, ctypes.c_int, P]),
+        "hg_world_upload_device": (ctypes.c_int, [P, ctypes.c_int, P]),
+        "hg_world_download_device": (ctypes.c_int, [P, ctypes.c_int, P]),
+        "hg_world_get_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
+        "hg_world_set_step": (ctypes.c_int, [P, ctypes.c_uint64]),
+        "hg_step": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "hg_sync": (ctypes.c_int, [P]),
+        "hg_world_totals": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def check(code):
+    if code != HG_OK:
+        raise HydrogenError(code, lib.hg_last_error().decode())
+    return code
+
+
+def header_functions(path=HEADER):
+    """Names of the functions declared in include/hydrogen.h."""
+    import re
+    text = open(path).read()
+    return sorted(set(re.findall(r"^\w[\w\s\*]*?\b(hg_\w+)\s*\(", text, re.M)))
+
+
+# ---- workload presets --------------------------------------------------------------
+TALUS_TAN = 0.65
+
+
+def settings_config1():
+    """Plain virtual-pipe erosion workload: dt 0.02, G 9.81, A = L = 1, Kc 0.1,
+    Ks = Kd = 0.05, Ke 0.015, thermal off (Kspeed 0), single material."""
+    s = ErosionSettings()
+    check(lib.hg_default_erosion_settings(ctypes.byref(s)))
+    s.Kc = 0.1
+    s.Ks[0] = s.Ks[1] = 0.05
+    s.Kd[0] = s.Kd[1] = 0.05
+    s.Ke = 0.015
+    s.ENERGY_KEPT = 1.0
+    s.G = 9.81
+    s.d_t = 0.02
+    s.Kconv = 0.0
+    s.Kalpha[0] = s.Kalpha[1] = math.atan(TALUS_TAN)
+    s.Kspeed[0] = s.Kspeed[1] = 0.0
+    return s
+
+
+def settings_config2():
+    """Config-1 physics with thermal erosion: talus tan 0.65, slippage 0.3."""
+    s = settings_config1()
+    s.Kspeed[0] = 0.3
+    return s
+
+
+def rain_uniform(amount=0.01, period=1):
+    r = RainSettings()
+    check(lib.hg_default_rain_settings(ctypes.byref(r)))
+    r.amount = amount
+    r.period = period
+    return r
+
+
+def options(rain_mode=RAIN_UNIFORM, p=0.0, seed=0, terrain_id=0, thermal=HG_AUTO, depth=HG_AUTO,
+            tile=(HG_AUTO, HG_AUTO)):
+    o = StepOptions()
+    check(lib.hg_default_step_options(ctypes.byref(o)))
+    o.rain_mode = rain_mode
+    o.rain_probability = p
+    o.rain_seed = seed
+    o.terrain_id = terrain_id
+    o.thermal = thermal
+    o.temporal_depth = depth
+    o.tile_x, o.tile_y = tile
+    return o
+
+
+def noise(seed=0, octaves=6, frequency=1.0 / 128, lacunarity=2.0, gain=0.5, lo=0.0, hi=64.0):
+    return NoiseSettings(seed, octaves, frequency, lacunarity, gain, lo, hi)
+
+
+def bernoulli_threshold(p):
+    t = math.floor(p * 4294967296.0)
+    return int(min(max(t, 0), 4294967295))
+
+
+class World:
+    """An n x n erosion world on the current CUDA device."""
+
+    def __init__(self, n, layers=1):
+        h = ctypes.c_void_p()
+        check(lib.hg_world_create(n, layers, ctypes.byref(h)))
+        self.h = h
+        self.n = n
+
+    def close(self):
+        if self.h:
+            lib.hg_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_erosion(self, s):
+        check(lib.hg_set_erosion_settings(self.h, ctypes.byref(s)))
+
+    def get_erosion(self):
+        s = ErosionSettings()
+        check(lib.hg_get_erosion_settings(self.h, ctypes.byref(s)))
+        return s
+
+    def set_rain(self, r):
+        check(lib.hg_set_rain_settings(self.h, ctypes.byref(r)))
+
+    def set_options(self, o):
+        check(lib.hg_set_step_options(self.h, ctypes.byref(o)))
+
+    def init_heightmap(self, ns):
+        check(lib.hg_init_heightmap(self.h, ctypes.byref(ns)))
+
+    def init_ks_field(self, ns, base, k):
+        check(lib.hg_init_ks_field(self.h, ctypes.byref(ns), base, k))
+
+    def clear_ks_field(self):
+        check(lib.hg_clear_ks_field(self.h))
+
+    def upload(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float32)
+        assert a.size == self.n * self.n
+        check(lib.hg_world_upload(self.h, FIELDS[field], a.ctypes.data))
+
+    def download(self, field):
+        a = np.empty((self.n, self.n), dtype=np.float32)
+        check(lib.hg_world_download(self.h, FIELDS[field], a.ctypes.data))
+        return a
+
+    def upload_device(self, field, ptr):
+        check(lib.hg_world_upload_device(self.h, FIELDS[field], ctypes.c_void_p(ptr)))
+
+    def download_device(self, field, ptr):
+        check(lib.hg_world_download_device(self.h, FIELDS[field], ctypes.c_void_p(ptr)))
+
+    def state(self, fields=STATE_FIELDS):
+        return {f: self.download(f) for f in fields}
+
+    def step(self, nsteps=1, mode=MODE_PLAIN):
+        check(lib.hg_step(self.h, nsteps, mode))
+
+    def sync(self):
+        check(lib.hg_sync(self.h))
+
+    @property
+    def step_count(self):
+        v = ctypes.c_uint64()
+        check(lib.hg_world_get_step(self.h, ctypes.byref(v)))
+        return v.value
+
+    @step_count.setter
+    def step_count(self, v):
+        check(lib.hg_world_set_step(self.h, v))
+
+    def totals(self):
+        out = (ctypes.c_double * 3)()
+        check(lib.hg_world_totals(self.h, out))
+        return list(out)
+
+    @property
+    def stream(self):
+        p = ctypes.c_void_p()
+        check(lib.hg_world_stream(self.h, ctypes.byref(p)))
+        return p.value or 0
+
+
+def configure(world, cfg, seed=0):
+    """Apply a named workload ('config1', 'config2') to a world."""
+    if cfg == "config1":
+        world.set_erosion(settings_config1())
+        world.set_rain(rain_uniform(0.01, 1))
+        world.set_options(options(RAIN_UNIFORM))
+    elif cfg == "config2":
+        world.set_erosion(settings_config2())
+        world.set_rain(rain_uniform(0.5, 1))
+        world.set_options(options(RAIN_BERNOULLI, p=0.001, seed=seed))
+    else:
+        raise ValueError(cfg)

@@ -1,0 +1,210 @@
+/* hydrogen.h — C ABI of the GB300 grid-erosion library (libhydrogen_gb300.so).
+ *
+ * The library replaces hydro-gen's grid-erosion step (the virtual-pipe
+ * shallow-water model with hydraulic and thermal erosion) with hand-written
+ * CUDA kernels for sm_103a.  Each entry point below names the reference
+ * interface it replaces (paths inside the hydro-gen project).
+ *
+ * Conventions
+ *  - Every function returns an int status (HG_OK == 0, negative on error) and
+ *    never aborts; hg_last_error() describes the last failure of the calling
+ *    thread.
+ *  - A world lives on the CUDA device that was current when it was created and
+ *    owns one CUDA stream; all work on a world is stream-ordered and
+ *    asynchronous unless the function says it synchronises.  A world must not
+ *    be used from two host threads at once; distinct worlds may be.
+ *  - Fields are n*n float32 arrays, row-major, x fastest; "top" is +y.
+ *  - No torch or C++ types cross this boundary: plain pointers and sizes.
+ */
+#ifndef HYDROGEN_GB300_H
+#define HYDROGEN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define HG_OK 0
+#define HG_ERR_INVALID (-1)     /* bad argument or settings */
+#define HG_ERR_OOM (-2)         /* device or host allocation failed */
+#define HG_ERR_CUDA (-3)        /* a CUDA runtime call failed */
+#define HG_ERR_TIMEOUT (-4)     /* a bounded device wait gave up */
+#define HG_ERR_UNSUPPORTED (-5) /* valid request this build does not support */
+#define HG_ERR_IO (-6)          /* checkpoint file error */
+#define HG_ERR_STATE (-7)       /* call not valid in the current state */
+
+/* ---- settings ------------------------------------------------------------- */
+
+/* Mirror of Erosion_data (glsl/bindings.glsl:39-60): same field names, order
+ * and std140 offsets (96 bytes), so a caller can pass the reference's struct
+ * bytes unchanged.  Index [0] is the rock layer, [1] the dirt layer
+ * (src/rendering.cpp:214).  Kalpha is the talus angle in radians. */
+typedef struct hg_erosion_settings {
+    uint32_t particle_count; /*  0  must be 0: grid model */
+    float Kc;                /*  4  sediment capacity */
+    float Kalpha[2];         /*  8  talus angle per layer (radians) */
+    float Kconv;             /* 16  rock->dirt sediment conversion */
+    float _pad0;             /* 20  std140 alignment of the next vec2 */
+    float Ks[2];             /* 24  dissolve (solubility) per layer */
+    float Kd[2];             /* 32  deposit per layer */
+    float Ke;                /* 40  evaporation */
+    float ENERGY_KEPT;       /* 44  flux damping */
+    float Kspeed[2];         /* 48  thermal slippage speed per layer */
+    float G;                 /* 56  gravity */
+    float d_t;               /* 60  time step */
+    float density;           /* 64..88 particle-model fields, unused by the grid model */
+    float init_volume;
+    float friction;
+    float inertia;
+    float min_volume;
+    float min_velocity;
+    uint32_t ttl;            /* 88 */
+    uint32_t _pad1;          /* 92  std140 struct size is a multiple of 16 */
+} hg_erosion_settings;
+
+/* Mirror of Rain_data (glsl/bindings.glsl:62-68), 20 bytes.  The grid step
+ * uses `amount` and `period` (rain on step n, 1-based, when n % period == 0,
+ * src/main.cpp:315-319); the remaining fields describe the reference's
+ * noise-driven rain and are stored unchanged. */
+typedef struct hg_rain_settings {
+    float amount;
+    float mountain_thresh;
+    float mountain_multip;
+    int32_t period;
+    float drops;
+} hg_rain_settings;
+
+#define HG_RAIN_OFF 0       /* no rain pass */
+#define HG_RAIN_UNIFORM 1   /* every cell gains `amount` */
+#define HG_RAIN_BERNOULLI 2 /* a cell gains `amount` with probability p, drawn
+                               from Philox4x32-10 keyed (seed, step, cell) */
+
+#define HG_AUTO (-1)
+
+/* Options of the grid step that the reference fixes in code; kept out of
+ * hg_erosion_settings so the 96-byte mirror stays byte-compatible. */
+typedef struct hg_step_options {
+    int32_t rain_mode;        /* HG_RAIN_* (default HG_RAIN_OFF) */
+    float rain_probability;   /* Bernoulli probability per cell and step */
+    uint64_t rain_seed;       /* Philox key */
+    uint32_t terrain_id;      /* fourth Philox counter word */
+    int32_t thermal;          /* HG_AUTO: thermal passes run when Kspeed[0] != 0 */
+    int32_t temporal_depth;   /* fused mode: steps per launch, HG_AUTO = tuned */
+    int32_t tile_x;           /* fused mode tile width (HG_AUTO = tuned) */
+    int32_t tile_y;           /* fused mode tile height (HG_AUTO = tuned) */
+    int32_t reserved[6];
+} hg_step_options;
+
+/* Simplex fBm heightmap: octave o samples 2-D simplex noise at cell
+ * coordinates times frequency*lacunarity^o with amplitude gain^o and hash
+ * seed+o; the sum is min-max scaled to [out_min, out_max]. */
+typedef struct hg_noise_settings {
+    uint32_t seed;
+    int32_t octaves;
+    float frequency;
+    float lacunarity;
+    float gain;
+    float out_min;
+    float out_max;
+} hg_noise_settings;
+
+/* ---- fields ---------------------------------------------------------------- */
+#define HG_FIELD_ROCK 0      /* heightmap.r: terrain height */
+#define HG_FIELD_WATER 1     /* heightmap.b: water depth */
+#define HG_FIELD_SEDIMENT 2  /* sedimap.r: suspended sediment */
+#define HG_FIELD_FLUX_L 3    /* fluxmap.x */
+#define HG_FIELD_FLUX_R 4    /* fluxmap.y */
+#define HG_FIELD_FLUX_T 5    /* fluxmap.z (+y) */
+#define HG_FIELD_FLUX_B 6    /* fluxmap.w (-y) */
+#define HG_FIELD_VEL_U 7     /* velocitymap.x */
+#define HG_FIELD_VEL_V 8     /* velocitymap.y */
+#define HG_FIELD_VEL_Z 9     /* velocitymap.z = d1+d2 of the last plain step */
+#define HG_FIELD_KS 10       /* per-cell rock solubility (replaces Ks[0]) */
+#define HG_FIELD_COUNT 11
+
+#define HG_MODE_PLAIN 0 /* one kernel per GLSL pass */
+#define HG_MODE_FUSED 1 /* one fused, tiled kernel per step (or per T steps) */
+
+typedef struct hg_world hg_world;
+
+/* ---- library ------------------------------------------------------------------ */
+const char* hg_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* hg_last_error(void);
+/* Number of kernels this library has launched in the process. */
+uint64_t hg_launch_count(void);
+
+/* Reference grid-model defaults (src/state.cpp:81-92). */
+int hg_default_erosion_settings(hg_erosion_settings* out);
+/* Reference rain defaults (src/settings.hpp:16-21). */
+int hg_default_rain_settings(hg_rain_settings* out);
+int hg_default_step_options(hg_step_options* out);
+
+/* ---- world ------------------------------------------------------------------------- */
+/* Replaces State::World::gen_textures (src/state.cpp:3-44): allocates the
+ * device fields of an n x n world (n a positive multiple of 8,
+ * src/erosion.cpp:83-84) on the current device.  layers must be 1 (rock with
+ * an empty dirt layer).  All fields start at zero. */
+int hg_world_create(int n, int layers, hg_world** out);
+/* Replaces State::World::delete_textures (src/state.cpp:46-55). */
+int hg_world_destroy(hg_world* w);
+int hg_world_size(const hg_world* w, int* n);
+/* The CUDA stream (cudaStream_t) every call on this world is ordered on. */
+int hg_world_stream(const hg_world* w, void** stream);
+
+/* Replaces Erosion_settings::push_data / "Set Erosion settings"
+ * (src/settings.hpp:64-66, src/rendering.cpp:303-305).  Takes effect at the
+ * next step.  Rejects particle_count != 0, d_t <= 0 and, for one-layer
+ * worlds, Kconv != 0 or Kspeed[1] != 0 (those need the dirt layer). */
+int hg_set_erosion_settings(hg_world* w, const hg_erosion_settings* s);
+int hg_get_erosion_settings(const hg_world* w, hg_erosion_settings* s);
+/* Replaces Rain_settings::push_data (src/settings.hpp:22-24). */
+int hg_set_rain_settings(hg_world* w, const hg_rain_settings* s);
+int hg_set_step_options(hg_world* w, const hg_step_options* o);
+
+/* Replaces State::World::gen_heightmap (src/state.cpp:116-147): writes the
+ * simplex-fBm heightmap into ROCK, zeroes every other field and resets the
+ * step counter. */
+int hg_init_heightmap(hg_world* w, const hg_noise_settings* s);
+/* Writes a raw (unscaled) fBm field into KS scaled as
+ * base * exp(k * fbm / sum_of_amplitudes); used for per-cell solubility. */
+int hg_init_ks_field(hg_world* w, const hg_noise_settings* s, float base, float k);
+/* Drops the per-cell solubility field (Ks[0] applies again). */
+int hg_clear_ks_field(hg_world* w);
+
+/* Copy one field between caller-owned host memory (n*n floats) and the world.
+ * Synchronous with respect to the host.  Uploading ROCK or WATER is the
+ * equivalent of writing the heightmap texture. */
+int hg_world_upload(hg_world* w, int field, const float* host);
+int hg_world_download(hg_world* w, int field, float* host);
+/* Same with a device pointer (stream-ordered, asynchronous). */
+int hg_world_upload_device(hg_world* w, int field, const float* dev);
+int hg_world_download_device(hg_world* w, int field, float* dev);
+
+/* Steps completed since the last init (the reference's erosion_steps,
+ * src/main.cpp:311). */
+int hg_world_get_step(const hg_world* w, uint64_t* step);
+int hg_world_set_step(hg_world* w, uint64_t step);
+
+/* ---- the grid step ------------------------------------------------------------------ */
+/* Replaces Erosion::dispatch_grid_rain + Erosion::dispatch_grid
+ * (src/erosion.hpp:45-46, src/erosion.cpp:76-89, 158-200) called once per
+ * main-loop iteration (src/main.cpp:310-320): advances the world by nsteps
+ * steps of rain -> hydro_flux -> hydro_erosion -> sediment_transport ->
+ * thermal_erosion/thermal_transport.  mode selects the per-pass kernels or
+ * the fused kernel; both give bit-identical fields.  Asynchronous. */
+int hg_step(hg_world* w, int nsteps, int mode);
+/* Waits for the world's stream (the reference's glMemoryBarrier/glFinish). */
+int hg_sync(hg_world* w);
+
+/* FP64 totals over the grid, computed on the device:
+ * out[0] rock, out[1] water, out[2] sediment.  Synchronises. */
+int hg_world_totals(hg_world* w, double out[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYDROGEN_GB300_H */

@@ -1,0 +1,238 @@
+"""ctypes wrapper of the oracle library — TEST INFRASTRUCTURE ONLY.
+
+The oracle (hg_oracle.cpp) restates hydro-gen's GLSL grid-erosion passes on
+the CPU, in float (the reference's precision) or double.  Only tests, the
+smoke check and the benchmark's CPU-baseline legs use it, always as the
+checker or the timed CPU baseline, never as part of the product path.
+
+Parity is pinned by the hand-derived known-answer cases in
+tests/test_oracle_kat.py (the reference ships no tests or golden vectors).
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhg_oracle.so")
+
+FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_t": 5, "flux_b": 6,
+          "vel_u": 7, "vel_v": 8, "dirt": 9, "sediment_dirt": 10, "vel_z": 11, "total": 12}
+PASSES = {"rain": 0, "flux": 1, "erosion": 2, "sediment": 3, "thermal_flux": 4, "thermal_transport": 5,
+          "smoothing": 6}
+
+
+class OracleErosion(ctypes.Structure):
+    """Erosion_data, glsl/bindings.glsl:39-60 (std140, 96 bytes)."""
+    _fields_ = [("particle_count", ctypes.c_uint32), ("Kc", ctypes.c_float),
+                ("Kalpha", ctypes.c_float * 2), ("Kconv", ctypes.c_float), ("pad0", ctypes.c_float),
+                ("Ks", ctypes.c_float * 2), ("Kd", ctypes.c_float * 2), ("Ke", ctypes.c_float),
+                ("ENERGY_KEPT", ctypes.c_float), ("Kspeed", ctypes.c_float * 2), ("G", ctypes.c_float),
+                ("d_t", ctypes.c_float), ("density", ctypes.c_float), ("init_volume", ctypes.c_float),
+                ("friction", ctypes.c_float), ("inertia", ctypes.c_float), ("min_volume", ctypes.c_float),
+                ("min_velocity", ctypes.c_float), ("ttl", ctypes.c_uint32), ("pad1", ctypes.c_uint32)]
+
+
+class OracleOptions(ctypes.Structure):
+    _fields_ = [("rain_mode", ctypes.c_int32), ("rain_period", ctypes.c_int32), ("rain_amount", ctypes.c_float),
+                ("rain_threshold", ctypes.c_uint32), ("rain_seed", ctypes.c_uint64),
+                ("terrain_id", ctypes.c_uint32), ("skip_identity", ctypes.c_int32)]
+
+
+def build():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_oracle_build", os.path.join(HERE, "build.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m.build()
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        build()
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    sig = {
+        "hgo_create": (P, [ctypes.c_int, ctypes.c_int]),
+        "hgo_destroy": (None, [P]),
+        "hgo_set_field": (ctypes.c_int, [P, ctypes.c_int, P]),
+        "hgo_get_field": (ctypes.c_int, [P, ctypes.c_int, P]),
+        "hgo_set_ks_field": (ctypes.c_int, [P, P]),
+        "hgo_set_step": (None, [P, ctypes.c_uint64]),
+        "hgo_get_step": (ctypes.c_uint64, [P]),
+        "hgo_step": (ctypes.c_int, [P, ctypes.POINTER(OracleErosion), ctypes.POINTER(OracleOptions), ctypes.c_int]),
+        "hgo_pass": (ctypes.c_int, [P, ctypes.POINTER(OracleErosion), ctypes.POINTER(OracleOptions), ctypes.c_int,
+                                    ctypes.c_int]),
+        "hgo_get_thermal": (ctypes.c_int, [P, P, P]),
+        "hgo_totals": (None, [P, ctypes.POINTER(ctypes.c_double)]),
+        "hgo_atanf": (ctypes.c_float, [ctypes.c_float]),
+        "hgo_philox4x32_10": (None, [ctypes.POINTER(ctypes.c_uint32)] * 3),
+        "hgo_atan_monotone_violations": (ctypes.c_uint64, [ctypes.c_uint32, ctypes.c_uint32]),
+        "hgo_rain_word": (ctypes.c_uint32, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32,
+                                            ctypes.c_uint64]),
+        "hgo_simplex2f": (ctypes.c_float, [ctypes.c_float, ctypes.c_float, ctypes.c_uint32]),
+        "hgo_fbm_raw": (None, [P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_float,
+                               ctypes.c_float, ctypes.c_float]),
+        "hgo_fbm_scaled": (None, [P, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+        "hgo_num_threads": (ctypes.c_int, []),
+        "hgo_set_num_threads": (None, [ctypes.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def erosion_from(s):
+    """Copy any ctypes struct with Erosion_data's fields into an OracleErosion."""
+    o = OracleErosion()
+    ctypes.memmove(ctypes.byref(o), ctypes.byref(s), ctypes.sizeof(OracleErosion))
+    return o
+
+
+def bernoulli_threshold(p):
+    t = math.floor(p * 4294967296.0)
+    return int(min(max(t, 0), 4294967295))
+
+
+def options(rain_mode=1, period=1, amount=0.01, p=0.0, seed=0, terrain_id=0, skip_identity=1):
+    return OracleOptions(rain_mode, period, amount, bernoulli_threshold(p), seed, terrain_id, skip_identity)
+
+
+def settings_config1():
+    s = OracleErosion()
+    s.Kc = 0.1
+    s.Ks[0] = s.Ks[1] = 0.05
+    s.Kd[0] = s.Kd[1] = 0.05
+    s.Ke = 0.015
+    s.ENERGY_KEPT = 1.0
+    s.G = 9.81
+    s.d_t = 0.02
+    s.Kalpha[0] = s.Kalpha[1] = math.atan(0.65)
+    return s
+
+
+def settings_config2():
+    s = settings_config1()
+    s.Kspeed[0] = 0.3
+    return s
+
+
+def workload(cfg, seed=0):
+    """(settings, options) of a named workload, matching hydrogen.configure."""
+    if cfg == "config1":
+        return settings_config1(), options(1, 1, 0.01)
+    if cfg == "config2":
+        return settings_config2(), options(2, 1, 0.5, p=0.001, seed=seed)
+    raise ValueError(cfg)
+
+
+def fbm(n, seed=0, octaves=6, frequency=1.0 / 128, lacunarity=2.0, gain=0.5, lo=0.0, hi=64.0):
+    out = np.empty((n, n), dtype=np.float32)
+    lib.hgo_fbm_scaled(out.ctypes.data, n, seed, octaves, frequency, lacunarity, gain, lo, hi)
+    return out
+
+
+def fbm_raw(w, h, seed, octaves, frequency, lacunarity, gain):
+    out = np.empty((h, w), dtype=np.float32)
+    lib.hgo_fbm_raw(out.ctypes.data, w, h, seed, octaves, frequency, lacunarity, gain)
+    return out
+
+
+class OracleWorld:
+    def __init__(self, n, precision=64):
+        self.n = n
+        self.precision = precision
+        self.h = lib.hgo_create(n, precision)
+        if not self.h:
+            raise ValueError("oracle create failed")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib.hgo_destroy(self.h)
+            self.h = None
+
+    def set(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        assert a.size == self.n * self.n
+        assert lib.hgo_set_field(self.h, FIELDS[field], a.ctypes.data) == 0
+
+    def get(self, field):
+        a = np.empty((self.n, self.n), dtype=np.float64)
+        assert lib.hgo_get_field(self.h, FIELDS[field], a.ctypes.data) == 0
+        return a
+
+    def set_ks(self, ks):
+        if ks is None:
+            lib.hgo_set_ks_field(self.h, None)
+            return
+        self._ks = np.ascontiguousarray(ks, dtype=np.float32)
+        lib.hgo_set_ks_field(self.h, self._ks.ctypes.data)
+
+    @property
+    def step_count(self):
+        return lib.hgo_get_step(self.h)
+
+    @step_count.setter
+    def step_count(self, v):
+        lib.hgo_set_step(self.h, v)
+
+    def step(self, settings, opts, nsteps=1):
+        rc = lib.hgo_step(self.h, ctypes.byref(settings), ctypes.byref(opts), nsteps)
+        if rc != 0:
+            raise RuntimeError(f"oracle step failed ({rc})")
+
+    def run_pass(self, name, settings, opts=None, layer=0):
+        opts = opts or options()
+        assert lib.hgo_pass(self.h, ctypes.byref(settings), ctypes.byref(opts), PASSES[name], layer) == 0
+
+    def thermal(self):
+        c = np.empty((self.n, self.n, 4))
+        d = np.empty((self.n, self.n, 4))
+        lib.hgo_get_thermal(self.h, c.ctypes.data, d.ctypes.data)
+        return c, d
+
+    def totals(self):
+        out = (ctypes.c_double * 4)()
+        lib.hgo_totals(self.h, out)
+        return list(out)
+
+    def state(self, fields=("rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u",
+                            "vel_v")):
+        return {f: self.get(f) for f in fields}
+
+
+def atanf(x):
+    return lib.hgo_atanf(x)
+
+
+def rain_word(x, y, step, terrain, seed):
+    return lib.hgo_rain_word(x, y, step, terrain, seed)
+
+
+def philox(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib.hgo_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def atan_monotone_violations(lo_bits=0, hi_bits=0x7F800000):
+    """Number of consecutive positive float pairs (by bit pattern) in
+    [lo_bits, hi_bits] where the polynomial arctangent decreases."""
+    return lib.hgo_atan_monotone_violations(lo_bits, hi_bits)
+
+
+def num_threads():
+    return lib.hgo_num_threads()
+
+
+def set_num_threads(t):
+    lib.hgo_set_num_threads(t)
