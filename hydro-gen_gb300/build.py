@@ -41,6 +41,9 @@ def _stale(target, deps):
 
 def build(force=False, verbose=False, ptxas_info=False):
     os.makedirs(OBJ, exist_ok=True)
+    # objects compiled on another host architecture must not be linked here:
+    # without the library (a fresh checkout or copy) everything is rebuilt
+    force = force or not os.path.exists(LIB)
     hs = headers()
     jobs = []
     for src in sources():

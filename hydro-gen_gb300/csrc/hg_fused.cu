@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(256) k_fused(FusedArgs a) {
             // sediment_transport: bilinear gather of eroded sediment
             float px, py;
             backtrace(c, gx, gy, arr[A_U][si], arr[A_V][si], px, py);
-            int ix = (int)px, iy = (int)py;
+            int ix = min(max((int)px, 0), n - 1), iy = min(max((int)py, 0), n - 1);
             int lx = ix - gx0, ly = iy - gy0;  // region coords of the (ix, iy) tap
             float s00, s10, s01, s11;
             bool staged = lx >= 1 && lx + 1 <= RW - 2 && ly >= 1 && ly + 1 <= RH - 2;

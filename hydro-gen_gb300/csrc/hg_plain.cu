@@ -91,7 +91,7 @@ __global__ void k_sediment(StepConsts c, const float* __restrict__ u, const floa
     backtrace(c, x, y, u[i], v[i], px, py);
     int ix = (int)px, iy = (int)py;
     auto tap = [&](int xx, int yy) -> float {
-        return (xx < n && yy < n) ? sed[at(n, xx, yy)] : 0.0f;
+        return (xx >= 0 && xx < n && yy >= 0 && yy < n) ? sed[at(n, xx, yy)] : 0.0f;
     };
     sed_o[i] = bilinear_mix(px, py, tap(ix, iy), tap(ix + 1, iy), tap(ix, iy + 1), tap(ix + 1, iy + 1));
     water[i] = water[i] * c.evap;

@@ -99,10 +99,13 @@ def test_fused_far_backtrace_fallback():
     step's input fields and must still match the per-pass kernels exactly."""
     n = 128
     rng = np.random.default_rng(3)
-    state = {"rock": rng.random((n, n)) * 10, "water": rng.random((n, n)) * 1e-3 + 1e-4,
+    state = {"rock": rng.random((n, n)) * 10, "water": np.full((n, n), 1e-3),
              "sediment": rng.random((n, n)) * 0.1}
-    for f in ("flux_l", "flux_r", "flux_t", "flux_b"):
-        state[f] = rng.random((n, n)) * 5.0
+    # outflow only from even columns / rows: those cells get no inflow, their
+    # water drains to ~0 and u = fR / d1 reaches ~100 cells per step
+    fr = np.zeros((n, n)); fr[:, ::2] = rng.random((n, n // 2)) * 5
+    ft = np.zeros((n, n)); ft[::2, :] = rng.random((n // 2, n)) * 5
+    state.update(flux_r=fr, flux_t=ft)
     worlds = []
     for mode in (H.MODE_PLAIN, H.MODE_FUSED):
         w = H.World(n)
@@ -112,7 +115,7 @@ def test_fused_far_backtrace_fallback():
         w.step(1, mode)
         worlds.append(w)
     u = worlds[0].download("vel_u")
-    assert np.abs(u).max() * 0.02 > 8  # far beyond the 3-4 cell halo
+    assert np.mean(np.abs(u) * 0.02 > 4) > 0.1  # far beyond the 3-4 cell halo
     for f in STATE:
         assert np.array_equal(worlds[0].download(f), worlds[1].download(f)), f
 
