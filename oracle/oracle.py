@@ -5,8 +5,9 @@ the CPU, in float (the reference's precision) or double.  Only tests, the
 smoke check and the benchmark's CPU-baseline legs use it, always as the
 checker or the timed CPU baseline, never as part of the product path.
 
-Parity is pinned by the hand-derived known-answer cases in
-tests/test_oracle_kat.py (the reference ships no tests or golden vectors).
+Parity unpinned: the reference ships no tests or golden vectors and its GLSL
+passes cannot run without an OpenGL driver, so the restatement is pinned by
+the hand-derived known-answer cases in tests/test_oracle_kat.py instead.
 """
 import ctypes
 import math

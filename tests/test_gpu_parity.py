@@ -144,25 +144,49 @@ def rel_err(w, ow):
 
 
 def test_fp64_tolerance_config1_256():
+    """100 steps: within 1e-4 of the height range of FP64.  1000 steps: the
+    reference's own float arithmetic drifts from FP64 by 1.04e-3 of the range
+    at one cell (chaotic growth from ~1.6e-6 at step 100; the median cell
+    stays near 7e-7), so the bar there is bit-identity with the float
+    restatement, with the FP64 deviation bounded at 2e-3 and reported."""
     w, ow, s, o = make_pair(256, "config1", prec=64)
+    f32 = O.OracleWorld(256, 32)
+    f32.set("rock", w.download("rock"))
     w.step(100, H.MODE_FUSED)
     ow.step(s, o, 100)
     e100 = rel_err(w, ow)
     assert e100 <= 1e-4, e100
     w.step(900, H.MODE_FUSED)
     ow.step(s, o, 900)
+    f32.step(s, o, 1000)
+    assert_bitwise(w, f32, ctx="1000 steps")
     e1000 = rel_err(w, ow)
-    assert e1000 <= 1e-3, e1000
+    assert e1000 <= 2e-3, e1000
     print(f"config1 256^2 rock error vs FP64: {e100:.3e} @100, {e1000:.3e} @1000")
 
 
 def test_fp64_tolerance_config2_256():
+    """Bernoulli rain leaves thin water films where the reference's velocity
+    (old-flux difference / depth) is ill-conditioned: in FP64 depths fall to
+    ~1e-51 and velocities reach ~1e134 while the same cells underflow to 0 in
+    float.  The float restatement itself therefore deviates from FP64 by
+    1.7e-3 of the height range at a few dozen cells after 100 steps.  Bar:
+    bit-identity with the float restatement, the 99.9th percentile of the
+    FP64 deviation within 1e-4, the maximum reported and bounded at 5e-3."""
     w, ow, s, o = make_pair(256, "config2", prec=64)
+    f32 = O.OracleWorld(256, 32)
+    f32.set("rock", w.download("rock"))
     w.step(100, H.MODE_FUSED)
     ow.step(s, o, 100)
-    e100 = rel_err(w, ow)
-    assert e100 <= 1e-4, e100
-    print(f"config2 256^2 rock error vs FP64: {e100:.3e} @100")
+    f32.step(s, o, 100)
+    assert_bitwise(w, f32, ctx="100 steps")
+    g = w.download("rock").astype(np.float64)
+    r = ow.get("rock")
+    e = np.abs(g - r) / (r.max() - r.min())
+    assert np.quantile(e, 0.999) <= 1e-4, np.quantile(e, 0.999)
+    assert e.max() <= 5e-3, e.max()
+    print(f"config2 256^2 rock error vs FP64 @100: max {e.max():.3e}, p99.9 {np.quantile(e, 0.999):.3e}, "
+          f"cells > 1e-4: {int(np.sum(e > 1e-4))}")
 
 
 def test_totals_match_oracle():
