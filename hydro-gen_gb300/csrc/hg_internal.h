@@ -62,4 +62,7 @@ int reduction_parts();
 // host copy of the polynomial arctangent (same operations as poly_atanf)
 float host_poly_atanf(float x);
 
+// Records msg as this thread's hg_last_error() and returns code.
+int hg_report_error(int code, const char* msg);
+
 }  // namespace hg

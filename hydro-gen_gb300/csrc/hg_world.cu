@@ -245,6 +245,8 @@ float* field_ptr(hg_world* w, int field) {
 
 }  // namespace
 
+int hg::hg_report_error(int code, const char* msg) { return fail(code, msg); }
+
 extern "C" {
 
 const char* hg_version(void) { return "hydrogen-gb300 0.1 (sm_103a)"; }

@@ -100,6 +100,7 @@ def _load():
         "hg_step": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
         "hg_sync": (ctypes.c_int, [P]),
         "hg_world_totals": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double)]),
+        "hg_field_totals_noalloc": (ctypes.c_int, [ctypes.POINTER(P), ctypes.c_int, ctypes.c_size_t, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -204,6 +204,27 @@ int hg_sync(hg_world* w);
  * out[0] rock, out[1] water, out[2] sediment.  Synchronises. */
 int hg_world_totals(hg_world* w, double out[3]);
 
+/* ---- allocation-free totals -------------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a host application that owns the device memory budget and lends plugins
+ * only its own buffers, or a frame loop that cannot take cudaMalloc's
+ * device-wide synchronisation): out[i] = FP64 sum of the `count` floats at
+ * device pointer fields[i], for i < nfields <= HG_NOALLOC_MAX_FIELDS, the
+ * same reduction as hg_world_totals.  fields is a host array of device
+ * pointers; out is device memory for nfields doubles, written on `stream`
+ * (a cudaStream_t, NULL for the legacy default stream); asynchronous.
+ * Allocates nothing: the partial sums live in a fixed library-global device
+ * array of HG_NOALLOC_MAX_FIELDS * 304 doubles (19,456 bytes) that each GPU
+ * loading the library holds until the process exits.  The first call on a
+ * device looks up that array's device address (once per device, with the
+ * device current), so make the first call on each device before any stream
+ * capture.  All calls share the one array: calls whose work overlaps on the
+ * GPU (different streams, no ordering between them) race and give wrong
+ * sums; order them on one stream or with events.  Rejects nfields outside
+ * [1, HG_NOALLOC_MAX_FIELDS] with HG_ERR_INVALID. */
+#define HG_NOALLOC_MAX_FIELDS 8
+int hg_field_totals_noalloc(const float* const* fields, int nfields, size_t count, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
