@@ -117,7 +117,8 @@ __device__ __forceinline__ FluxOut cell_flux(const StepConsts& c, int x, int y,
                                              float w_c, float d1,
                                              float fl, float fr, float ft, float fb,
                                              float wl, float wr, float wt, float wb,
-                                             float inl, float inr, float int_, float inb) {
+                                             float inl, float inr, float int_, float inb,
+                                             bool border = true) {
     FluxOut o;
     // :88-92 total height differences; :100-107 new outflow (A == L == 1, the
     // products and quotients by 1 are exact and dropped)
@@ -126,15 +127,22 @@ __device__ __forceinline__ FluxOut cell_flux(const StepConsts& c, int x, int y,
     o.fr = gmax(0.0f, c.EK * fr + c.dt * (c.G * dhr));
     o.ft = gmax(0.0f, c.EK * ft + c.dt * (c.G * dht));
     o.fb = gmax(0.0f, c.EK * fb + c.dt * (c.G * dhb));
-    // :110-119 closed boundaries
-    if (x <= 0) o.fl = 0.0f;
-    else if (x >= c.n - 1) o.fr = 0.0f;
-    if (y <= 0) o.fb = 0.0f;
-    else if (y >= c.n - 1) o.ft = 0.0f;
+    // :110-119 closed boundaries (callers that never see the grid edge pass
+    // border = false)
+    if (border) {
+        if (x <= 0) o.fl = 0.0f;
+        else if (x >= c.n - 1) o.fr = 0.0f;
+        if (y <= 0) o.fb = 0.0f;
+        else if (y >= c.n - 1) o.ft = 0.0f;
+    }
     // :121-127 scale outflow to the available water
     float sum_in = inl + inr + int_ + inb;
     float sum_out = o.fl + o.fr + o.ft + o.fb;
-    float K = gmin(1.0f, d1 / (sum_out * c.dt));
+    // K = min(1, d1 / den).  d1 >= den means the exact quotient is >= 1 (or
+    // 0/0, inf/inf: NaN, which GLSL's min also maps to 1), so K = 1 without
+    // dividing; otherwise the division decides.
+    float den = sum_out * c.dt;
+    float K = d1 >= den ? 1.0f : gmin(1.0f, d1 / den);
     o.fl *= K; o.fr *= K; o.ft *= K; o.fb *= K;
     sum_out *= K;
     // :133-134 water update

@@ -40,7 +40,8 @@ struct FusedArgs {
     StateBufs in, out;
     float* u;
     float* v;
-    int* overflow;  // set when a back-trace leaves the staged tile (T > 1 only)
+    float* s_ero;  // eroded sediment of every cell (k_hydro -> k_transport)
+    float* b_ero;  // eroded rock of every cell (k_hydro -> k_transport, thermal on)
 };
 int fused_max_depth();
 void launch_fused(const FusedArgs& a, int depth, int tile_x, int tile_y, cudaStream_t st);

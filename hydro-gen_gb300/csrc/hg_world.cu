@@ -71,7 +71,8 @@ struct hg_world {
     float4* td = nullptr;
     float* ks = nullptr;
     bool ks_on = false;
-    int* flags = nullptr;
+    float* s_ero = nullptr;  // fused step: eroded sediment of every cell
+    float* b_ero = nullptr;  // fused step: eroded rock of every cell
     float* red_f = nullptr;   // min/max partials + result
     double* red_d = nullptr;  // FP64 partials + result
 };
@@ -121,7 +122,8 @@ void free_world(hg_world* w) {
     }
     cudaFree(w->u); cudaFree(w->v); cudaFree(w->vz);
     cudaFree(w->tc); cudaFree(w->td);
-    cudaFree(w->ks); cudaFree(w->flags);
+    cudaFree(w->ks);
+    cudaFree(w->s_ero); cudaFree(w->b_ero);
     cudaFree(w->red_f); cudaFree(w->red_d);
     if (w->stream) cudaStreamDestroy(w->stream);
 }
@@ -216,7 +218,7 @@ RainStep make_rain(const hg_world* w, uint64_t step1) {
 }
 
 bool pick_tile(const hg_world* w, int& tx, int& ty) {
-    const int cand[][2] = {{64, 32}, {64, 16}, {32, 32}};
+    const int cand[][2] = {{64, 16}};
     if (w->opt.tile_x > 0 && w->opt.tile_y > 0) {
         tx = w->opt.tile_x; ty = w->opt.tile_y;
         return fused_supported(1, tx, ty) && w->n % tx == 0 && w->n % ty == 0;
@@ -320,7 +322,8 @@ int hg_world_create(int n, int layers, hg_world** out) {
     if (e == cudaSuccess) e = alloc((void**)&w->tc, 4 * bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->td, 4 * bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->ks, bytes);
-    if (e == cudaSuccess) e = alloc((void**)&w->flags, 64);
+    if (e == cudaSuccess) e = alloc((void**)&w->s_ero, bytes);
+    if (e == cudaSuccess) e = alloc((void**)&w->b_ero, bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->red_f, sizeof(float) * (2 * reduction_parts() + 2));
     if (e == cudaSuccess) e = alloc((void**)&w->red_d, sizeof(double) * (8 * reduction_parts() + 8));
     if (e != cudaSuccess) {
@@ -337,7 +340,6 @@ int hg_world_create(int n, int layers, hg_world** out) {
     cudaMemsetAsync(w->u, 0, bytes, w->stream);
     cudaMemsetAsync(w->v, 0, bytes, w->stream);
     cudaMemsetAsync(w->vz, 0, bytes, w->stream);
-    cudaMemsetAsync(w->flags, 0, 64, w->stream);
     e = cudaStreamSynchronize(w->stream);
     if (e != cudaSuccess) {
         free_world(w);
@@ -540,7 +542,7 @@ int hg_step(hg_world* w, int nsteps, int mode) {
     } else {
         int tx = 0, ty = 0;
         if (!pick_tile(w, tx, ty))
-            return fail(HG_ERR_UNSUPPORTED, "fused mode needs n divisible by a supported tile (64x32, 64x16, 32x32)");
+            return fail(HG_ERR_UNSUPPORTED, "fused mode needs n divisible by its 64x16 tile");
         for (int k = 0; k < nsteps; ++k) {
             FusedArgs a{};
             a.c = c;
@@ -548,7 +550,8 @@ int hg_step(hg_world* w, int nsteps, int mode) {
             for (int f = 0; f < S_COUNT; ++f) { a.in.f[f] = w->cur[f]; a.out.f[f] = w->alt[f]; }
             a.u = w->u;
             a.v = w->v;
-            a.overflow = w->flags;
+            a.s_ero = w->s_ero;
+            a.b_ero = w->b_ero;
             launch_fused(a, 1, tx, ty, st);
             for (int f = 0; f < S_COUNT; ++f) swap(f);
             w->step += 1;

@@ -82,15 +82,18 @@ def test_fused_bitwise_vs_float_oracle_thermal():
     assert_bitwise(w, ow)
 
 
-@pytest.mark.parametrize("tile", [(64, 32), (64, 16), (32, 32)])
-def test_fused_tiles_agree(tile):
+def test_fused_tile_option():
     a, _, _, _ = make_pair(256, "config2", p=0.01)
     b, _, _, _ = make_pair(256, "config2", p=0.01)
-    b.set_options(H.options(H.RAIN_BERNOULLI, p=0.01, tile=tile))
+    b.set_options(H.options(H.RAIN_BERNOULLI, p=0.01, tile=(64, 16)))
     a.step(40, H.MODE_PLAIN)
     b.step(40, H.MODE_FUSED)
     for f in STATE:
         assert np.array_equal(a.download(f), b.download(f)), f
+    b.set_options(H.options(H.RAIN_BERNOULLI, p=0.01, tile=(32, 32)))
+    with pytest.raises(H.HydrogenError) as e:
+        b.step(1, H.MODE_FUSED)
+    assert e.value.code == -5
 
 
 def test_fused_far_backtrace_fallback():
