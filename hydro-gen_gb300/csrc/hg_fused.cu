@@ -10,239 +10,398 @@
 // reach |u|*dt is unbounded (velocity divides by the water depth, and thin
 // films give reaches of thousands of cells), so no halo can hold it; after
 // k_hydro has written the eroded sediment of every cell, k_transport gathers
-// any tap straight from HBM/L2.  The split costs 16 B per cell-step of
+// any tap straight from L2/HBM.  The split costs 16 B per cell-step of
 // intermediate traffic (eroded rock and sediment written and read once) and
 // saves recomputing flux and erosion on a halo ring.
 //
-// k_hydro stages the tile's rock, water (+ this step's rain), and the four
-// fluxes with a 1-cell halo (4 columns for 16-byte rows) in shared memory:
-// one Philox call per four cells, coalesced float4 rows, then each thread
-// computes four cells.  k_transport stages eroded rock with a 2-cell halo,
-// computes each cell's eight talus outflows once (ring included) into shared
-// memory, then applies outflow and inflow and the sediment gather.
+// Both kernels work on 64 x 16 tiles with 256 threads; each thread owns a
+// row group of four horizontally adjacent cells, so neighbour values come
+// from float4 shared-memory rows and every HBM write is a float4.
+//   k_hydro stages rock, water and the four fluxes of the tile plus a halo
+//   (4 columns, 1 row) with six TMA 2-D tile loads; while they fly, threads
+//   draw this step's Philox rain words and load their own sediment; rain is
+//   then added in shared memory.
+//   k_transport stages the eroded rock with a 2-row halo by one TMA load,
+//   computes each cell's eight talus outflows once (the ring of interior
+//   plus 1 included) into shared memory, then applies outflow and inflow,
+//   and gathers the four sediment taps of every cell from HBM/L2.
 //
 // Per-cell arithmetic is the code of the per-pass kernels (hg_device.cuh),
 // so the fused step reproduces them bit for bit.
+#include <cudaTypedefs.h>
+
+#include <mutex>
+#include <vector>
+
 #include "hg_internal.h"
+#include "hg_tma.cuh"
 
 namespace hg {
 
 namespace {
 
 constexpr int TW = 64, TH = 16, NTH = 256;
-constexpr int CPT = TW * TH / NTH;  // cells per thread (4)
-constexpr int HX = 4;               // halo columns: 16-byte aligned rows
+constexpr int GPR = TW / 4;  // row groups per tile row (16)
+constexpr int HX = 4;        // halo columns: 16-byte aligned TMA boxes
+constexpr int RW = TW + 2 * HX;  // 72
 
+// k_hydro region: (TW + 8) x (TH + 2), origin (tx0 - 4, ty0 - 1)
+constexpr int H_RH = TH + 2, H_BOX = RW * H_RH;  // 1296 floats
+constexpr int H_RC = ((H_BOX + 31) / 32) * 32;   // 128-byte aligned array stride
+enum { H_B = 0, H_D, H_S, H_FL, H_FR, H_FT, H_FB, H_N };
+
+// k_transport region: (TW + 8) x (TH + 4), origin (tx0 - 4, ty0 - 2)
+constexpr int T_RH = TH + 4, T_BOX = RW * T_RH;  // 1440 floats
+// outflows of interior plus 1: region rows 1..TH+2, same column layout
+constexpr int O_RH = TH + 2, O_C = RW * O_RH;    // 1296 floats per direction
+
+// direction d: L, R, T, B, LT, RT, LB, RB; offsets and the opposite direction
 __constant__ int f_ox[8] = {-1, 1, 0, 0, -1, 1, -1, 1};
 __constant__ int f_oy[8] = {0, 0, 1, -1, 1, 1, -1, -1};
-// direction from a neighbour back to this cell: L<->R, T<->B, LT<->RB, RT<->LB
 __constant__ int f_opp[8] = {1, 0, 3, 2, 7, 6, 5, 4};
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float at4(const float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+
+__device__ __forceinline__ void report_timeout(const FusedArgs& a) {
+    if (threadIdx.x == 0) atomicExch(a.err, 1);
+}
 
 // ---------------------------------------------------------------------------
 // k_hydro
 // ---------------------------------------------------------------------------
-constexpr int H_RW = TW + 2 * HX, H_RH = TH + 2, H_RC = H_RW * H_RH;
-enum { H_B = 0, H_D, H_FL, H_FR, H_FT, H_FB, H_N };
-
 template <bool EDGE>
-__device__ __forceinline__ void hydro_tile(const FusedArgs& a, float* sm, int tx0, int ty0) {
+__device__ __forceinline__ void hydro_tile(const TmaMaps& maps, const FusedArgs& a, float* sm, uint64_t* bar,
+                                           int tx0, int ty0) {
     const StepConsts& c = a.c;
     const RainStep& r = a.rain[0];
     const int n = c.n;
     const int tid = threadIdx.x;
     const int gx0 = tx0 - HX, gy0 = ty0 - 1;
-    const float* src[H_N] = {a.in.f[S_ROCK], a.in.f[S_WATER], a.in.f[S_FL], a.in.f[S_FR], a.in.f[S_FT],
-                             a.in.f[S_FB]};
-    constexpr int G4 = H_RW / 4;
-    for (int q = tid; q < G4 * H_RH; q += NTH) {
-        int ry = q / G4, rx = (q % G4) * 4;
-        int gx = gx0 + rx, gy = gy0 + ry;
-        bool ok = !EDGE || (gx >= 0 && gx < n && gy >= 0 && gy < n);
-        size_t gi = (size_t)gy * n + gx;
-        int si = ry * H_RW + rx;
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, H_N * H_BOX * sizeof(float));
 #pragma unroll
-        for (int f = 0; f < H_N; ++f) {
-            float4 v = ok ? __ldg(reinterpret_cast<const float4*>(src[f] + gi)) : make_float4(0, 0, 0, 0);
-            if (f == H_D && ok && r.active) {
-                uint32_t w[4] = {0, 0, 0, 0};
-                if (r.bernoulli) rain_words4(r, gx, gy, w);
-                v.x += rain_incr(r, w[0]);
-                v.y += rain_incr(r, w[1]);
-                v.z += rain_incr(r, w[2]);
-                v.w += rain_incr(r, w[3]);
-            }
-            *reinterpret_cast<float4*>(sm + f * H_RC + si) = v;
+        for (int f = 0; f < H_N; ++f) tma_load_2d(sm + f * H_RC, &maps.m[f], gx0, gy0, bar);
+    }
+    // rain words of the region's row groups (18 rows x 18 groups), drawn while the tiles load
+    constexpr int RG = (RW / 4) * H_RH;  // 324
+    uint32_t words[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        int q = tid + k * NTH;
+        if (q < RG && r.active && r.bernoulli) {
+            int gx = gx0 + (q % (RW / 4)) * 4, gy = gy0 + q / (RW / 4);
+            if (!EDGE || (gx >= 0 && gx < n && gy >= 0 && gy < n)) rain_words4(r, gx, gy, words[k]);
+        }
+    }
+    bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    if (!ok) {  // the tile never arrived: record, give the copies one more bounded wait, skip the tile
+        report_timeout(a);
+        mbar_wait(bar, 0);
+        return;
+    }
+    if (r.active) {
+        float* D = sm + H_D * H_RC;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            int q = tid + k * NTH;
+            if (q >= RG) continue;
+            int rx = (q % (RW / 4)) * 4, ry = q / (RW / 4);
+            int gx = gx0 + rx, gy = gy0 + ry;
+            if (EDGE && !(gx >= 0 && gx < n && gy >= 0 && gy < n)) continue;
+            float4 d = ld4(D + ry * RW + rx);
+            d.x += rain_incr(r, words[k][0]);
+            d.y += rain_incr(r, words[k][1]);
+            d.z += rain_incr(r, words[k][2]);
+            d.w += rain_incr(r, words[k][3]);
+            st4(D + ry * RW + rx, d);
         }
     }
     __syncthreads();
+
     const float* B = sm + H_B * H_RC;
     const float* D = sm + H_D * H_RC;
+    const float* S = sm + H_S * H_RC;
     const float* FL = sm + H_FL * H_RC;
     const float* FR = sm + H_FR * H_RC;
     const float* FT = sm + H_FT * H_RC;
     const float* FB = sm + H_FB * H_RC;
+    // one cell per iteration (low register use keeps ~5 blocks per SM to hide
+    // the long dependent chains of flux and erosion); a warp covers 32
+    // consecutive cells of a row
 #pragma unroll 1
-    for (int k = 0; k < CPT; ++k) {
-        int q = tid + k * NTH;
-        int rx = HX + q % TW, ry = 1 + q / TW;
-        int gx = gx0 + rx, gy = gy0 + ry;
-        int si = ry * H_RW + rx;
-        size_t gi = (size_t)gy * n + gx;
-        auto tot = [&](int dx, int dy) -> float {
-            if (EDGE) {
-                int xx = gx + dx, yy = gy + dy;
-                if (xx < 0 || xx >= n || yy < 0 || yy >= n) return FAR_HEIGHT;
-            }
-            int j = si + dy * H_RW + dx;
-            return B[j] + D[j];
-        };
-        float d1 = D[si];
-        float b = B[si];
+    for (int k = 0; k < TW * TH / NTH; ++k) {
+        const int q = tid + k * NTH;
+        const int ix = q % TW, iy = q / TW;
+        const int x = tx0 + ix, y = ty0 + iy;
+        const int si = (1 + iy) * RW + HX + ix;
+        const size_t gi = (size_t)y * n + x;
+        const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
+        const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
+        float b = B[si], d1 = D[si];
+        float bl = B[si - 1], br = B[si + 1], bb = B[si - RW], bt = B[si + RW];
         float w_c = b + d1;
-        float inl = (!EDGE || gx > 0) ? FR[si - 1] : 0.0f;
-        float inr = (!EDGE || gx < n - 1) ? FL[si + 1] : 0.0f;
-        float int_ = (!EDGE || gy < n - 1) ? FB[si + H_RW] : 0.0f;
-        float inb = (!EDGE || gy > 0) ? FT[si - H_RW] : 0.0f;
-        FluxOut o = cell_flux(c, gx, gy, w_c, d1, FL[si], FR[si], FT[si], FB[si], tot(-1, 0), tot(1, 0), tot(0, 1),
-                              tot(0, -1), inl, inr, int_, inb, EDGE);
-        float s = __ldg(a.in.f[S_SED] + gi);
-        float br = (!EDGE || gx < n - 1) ? B[si + 1] : 0.0f;
-        float bl = (!EDGE || gx > 0) ? B[si - 1] : 0.0f;
-        float bb = (!EDGE || gy > 0) ? B[si - H_RW] : 0.0f;
-        float bt = (!EDGE || gy < n - 1) ? B[si + H_RW] : 0.0f;
+        float wl = has_l ? bl + D[si - 1] : FAR_HEIGHT;
+        float wr = has_r ? br + D[si + 1] : FAR_HEIGHT;
+        float wt = has_t ? bt + D[si + RW] : FAR_HEIGHT;
+        float wb = has_b ? bb + D[si - RW] : FAR_HEIGHT;
+        float inl = has_l ? FR[si - 1] : 0.0f;
+        float inr = has_r ? FL[si + 1] : 0.0f;
+        float int_ = has_t ? FB[si + RW] : 0.0f;
+        float inb = has_b ? FT[si - RW] : 0.0f;
+        FluxOut o = cell_flux(c, x, y, w_c, d1, FL[si], FR[si], FT[si], FB[si], wl, wr, wt, wb, inl, inr, int_, inb,
+                              EDGE);
+        float s = S[si];
         float Kls0 = c.ks_field ? c.dt * __ldg(c.ks_field + gi) : c.Kls0;
-        cell_erosion(c, Kls0, o.u, o.v, o.vz, b, s, br, bl, bb, bt);
+        cell_erosion(c, Kls0, o.u, o.v, o.vz, b, s, has_r ? br : 0.0f, has_l ? bl : 0.0f, has_b ? bb : 0.0f,
+                     has_t ? bt : 0.0f);
         a.out.f[S_FL][gi] = o.fl;
         a.out.f[S_FR][gi] = o.fr;
         a.out.f[S_FT][gi] = o.ft;
         a.out.f[S_FB][gi] = o.fb;
-        a.out.f[S_WATER][gi] = o.d2 * c.evap;  // sediment_transport's evaporation (:75)
+        a.out.f[S_WATER][gi] = o.d2 * c.evap;  // sediment_transport's evaporation (glsl/sediment_transport.glsl:75)
         a.u[gi] = o.u;
         a.v[gi] = o.v;
         a.s_ero[gi] = s;
-        if (c.thermal) a.b_ero[gi] = b;
-        else a.out.f[S_ROCK][gi] = b;  // no thermal pass: eroded rock is final
+        (c.thermal ? a.b_ero : a.out.f[S_ROCK])[gi] = b;  // no thermal pass: eroded rock is final
     }
 }
 
-__global__ void __launch_bounds__(NTH) k_hydro(FusedArgs a) {
-    __shared__ __align__(16) float sm[H_N * H_RC];
+__global__ void __launch_bounds__(NTH) k_hydro(const __grid_constant__ TmaMaps maps, const __grid_constant__ FusedArgs a) {
+    __shared__ __align__(128) float sm[H_N * H_RC];
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
     const int n = a.c.n;
     const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 1 >= 0 && ty0 + TH + 1 <= n;
-    if (inner) hydro_tile<false>(a, sm, tx0, ty0);
-    else hydro_tile<true>(a, sm, tx0, ty0);
+    if (inner) hydro_tile<false>(maps, a, sm, &bar, tx0, ty0);
+    else hydro_tile<true>(maps, a, sm, &bar, tx0, ty0);
 }
 
 // ---------------------------------------------------------------------------
 // k_transport
 // ---------------------------------------------------------------------------
-constexpr int T_RW = TW + 2 * HX, T_RH = TH + 4, T_RC = T_RW * T_RH;
-// outflows are kept for interior plus 1: (TW + 2) x (TH + 2) cells
-constexpr int O_W = TW + 2, O_H = TH + 2, O_C = O_W * O_H;
+
+// Eight talus outflows of the cell at region (rx, ry) from the staged eroded
+// rock (FAR_HEIGHT outside the grid); the shader's thermal_erosion pass.
+template <bool EDGE>
+__device__ __forceinline__ void outflows_scalar(const StepConsts& c, const float* be, int rx, int ry, int gx,
+                                                int gy, float o8[8]) {
+    const int n = c.n;
+    if (EDGE && (gx < 0 || gx >= n || gy < 0 || gy >= n)) {
+#pragma unroll
+        for (int d = 0; d < 8; ++d) o8[d] = 0.0f;
+        return;
+    }
+    const int si = ry * RW + rx;
+    const float b = be[si];
+    float nb[8];
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {
+        bool out = false;
+        if (EDGE) {
+            int xx = gx + f_ox[d], yy = gy + f_oy[d];
+            out = xx < 0 || xx >= n || yy < 0 || yy >= n;
+        }
+        nb[d] = out ? FAR_HEIGHT : be[si + f_oy[d] * RW + f_ox[d]];
+    }
+    ThermalOut t = cell_thermal_fast(c, b, nb);
+#pragma unroll
+    for (int d = 0; d < 8; ++d) o8[d] = (t.mask >> d & 1u) ? t.S * (b - nb[d]) / t.bk : 0.0f;
+}
 
 template <bool EDGE>
-__device__ __forceinline__ void transport_tile(const FusedArgs& a, float* be, float* outf, int tx0, int ty0) {
+__device__ __forceinline__ void transport_tile(const TmaMaps& maps, const FusedArgs& a, float* be, float* outf,
+                                               uint64_t* bar, int tx0, int ty0) {
     const StepConsts& c = a.c;
     const int n = c.n;
     const int tid = threadIdx.x;
     const int gx0 = tx0 - HX, gy0 = ty0 - 2;
-    if (c.thermal) {
-        constexpr int G4 = T_RW / 4;
-        for (int q = tid; q < G4 * T_RH; q += NTH) {
-            int ry = q / G4, rx = (q % G4) * 4;
-            int gx = gx0 + rx, gy = gy0 + ry;
-            bool ok = !EDGE || (gx >= 0 && gx < n && gy >= 0 && gy < n);
-            float4 v = ok ? __ldg(reinterpret_cast<const float4*>(a.b_ero + (size_t)gy * n + gx))
-                          : make_float4(0, 0, 0, 0);
-            *reinterpret_cast<float4*>(be + ry * T_RW + rx) = v;
-        }
-        __syncthreads();
-        // eight outflows of every cell of interior plus 1 (the shader's
-        // thermal_erosion pass), each directed edge's division done once
-        for (int q = tid; q < O_C; q += NTH) {
-            int ox = q % O_W, oy = q / O_W;
-            int rx = HX - 1 + ox, ry = 1 + oy;
-            int gx = gx0 + rx, gy = gy0 + ry;
-            float o8[8];
-            if (EDGE && (gx < 0 || gx >= n || gy < 0 || gy >= n)) {
-#pragma unroll
-                for (int d = 0; d < 8; ++d) o8[d] = 0.0f;
-            } else {
-                int si = ry * T_RW + rx;
-                float b = be[si];
-                float nb[8];
-#pragma unroll
-                for (int d = 0; d < 8; ++d) {
-                    bool out = false;
-                    if (EDGE) {
-                        int xx = gx + f_ox[d], yy = gy + f_oy[d];
-                        out = xx < 0 || xx >= n || yy < 0 || yy >= n;
-                    }
-                    nb[d] = out ? FAR_HEIGHT : be[si + f_oy[d] * T_RW + f_ox[d]];
-                }
-                ThermalOut t = cell_thermal_fast(c, b, nb);
-#pragma unroll
-                for (int d = 0; d < 8; ++d) o8[d] = (t.mask >> d & 1u) ? t.S * (b - nb[d]) / t.bk : 0.0f;
-            }
-#pragma unroll
-            for (int d = 0; d < 8; ++d) outf[d * O_C + q] = o8[d];
-        }
-        __syncthreads();
+    if (c.thermal && tid == 0) {
+        mbar_arrive_expect_tx(bar, T_BOX * sizeof(float));
+        tma_load_2d(be, &maps.m[H_N], gx0, gy0, bar);
     }
-#pragma unroll 1
-    for (int k = 0; k < CPT; ++k) {
-        int q = tid + k * NTH;
-        int ix0 = q % TW, iy0 = q / TW;
-        int gx = tx0 + ix0, gy = ty0 + iy0;
-        size_t gi = (size_t)gy * n + gx;
-        // sediment_transport: semi-Lagrangian gather of eroded sediment
+    const int iy = tid / GPR, g = tid % GPR;
+    const int x0 = tx0 + 4 * g, y = ty0 + iy;
+    const size_t gi0 = (size_t)y * n + x0;
+    const float4 u4 = __ldg(reinterpret_cast<const float4*>(a.u + gi0));
+    const float4 v4 = __ldg(reinterpret_cast<const float4*>(a.v + gi0));
+
+    // sediment_transport: semi-Lagrangian gather of eroded sediment (any reach)
+    float sed[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
         float px, py;
-        backtrace(c, gx, gy, __ldg(a.u + gi), __ldg(a.v + gi), px, py);
-        int ix = min(max((int)px, 0), n - 1), iy = min(max((int)py, 0), n - 1);
-        const float* se = a.s_ero + (size_t)iy * n + ix;
+        backtrace(c, x0 + j, y, at4(u4, j), at4(v4, j), px, py);
+        int ix = min(max((int)px, 0), n - 1), iy2 = min(max((int)py, 0), n - 1);
+        const float* se = a.s_ero + (size_t)iy2 * n + ix;
         float s00 = __ldg(se);
         float s10 = ix + 1 < n ? __ldg(se + 1) : 0.0f;
-        float s01 = iy + 1 < n ? __ldg(se + n) : 0.0f;
-        float s11 = (ix + 1 < n && iy + 1 < n) ? __ldg(se + n + 1) : 0.0f;
-        a.out.f[S_SED][gi] = bilinear_mix(px, py, s00, s10, s01, s11);
-        // thermal_transport: own outflows out, neighbours' outflows in
-        if (c.thermal) {
-            int oi = (iy0 + 1) * O_W + (ix0 + 1);
+        float s01 = iy2 + 1 < n ? __ldg(se + n) : 0.0f;
+        float s11 = (ix + 1 < n && iy2 + 1 < n) ? __ldg(se + n + 1) : 0.0f;
+        sed[j] = bilinear_mix(px, py, s00, s10, s01, s11);
+    }
+    *reinterpret_cast<float4*>(a.out.f[S_SED] + gi0) = make_float4(sed[0], sed[1], sed[2], sed[3]);
+    if (!c.thermal) return;
+
+    bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    if (!ok) {
+        report_timeout(a);
+        mbar_wait(bar, 0);
+        return;
+    }
+    // ---- outflows of the interior row groups (one per thread) --------------
+    const int rx0 = HX + 4 * g, ry = 2 + iy;  // region coords of the group's first cell
+    {
+        const int si = ry * RW + rx0;
+        const float4 m4 = ld4(be + si - RW), c4 = ld4(be + si), p4 = ld4(be + si + RW);
+        const float ml = be[si - RW - 1], mr = be[si - RW + 4];
+        const float cl = be[si - 1], cr = be[si + 4];
+        const float pl = be[si + RW - 1], pr = be[si + RW + 4];
+        float o[8][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int x = x0 + j;
+            const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
+            const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
+            float nb[8];
+            nb[0] = has_l ? (j == 0 ? cl : at4(c4, j - 1)) : FAR_HEIGHT;
+            nb[1] = has_r ? (j == 3 ? cr : at4(c4, j + 1)) : FAR_HEIGHT;
+            nb[2] = has_t ? at4(p4, j) : FAR_HEIGHT;
+            nb[3] = has_b ? at4(m4, j) : FAR_HEIGHT;
+            nb[4] = (has_l && has_t) ? (j == 0 ? pl : at4(p4, j - 1)) : FAR_HEIGHT;
+            nb[5] = (has_r && has_t) ? (j == 3 ? pr : at4(p4, j + 1)) : FAR_HEIGHT;
+            nb[6] = (has_l && has_b) ? (j == 0 ? ml : at4(m4, j - 1)) : FAR_HEIGHT;
+            nb[7] = (has_r && has_b) ? (j == 3 ? mr : at4(m4, j + 1)) : FAR_HEIGHT;
+            const float b = at4(c4, j);
+            ThermalOut t = cell_thermal_fast(c, b, nb);
+#pragma unroll
+            for (int d = 0; d < 8; ++d) o[d][j] = (t.mask >> d & 1u) ? t.S * (b - nb[d]) / t.bk : 0.0f;
+        }
+        const int oi = (ry - 1) * RW + rx0;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) st4(outf + d * O_C + oi, make_float4(o[d][0], o[d][1], o[d][2], o[d][3]));
+    }
+    // ---- outflows of the ring of interior plus 1 ---------------------------
+    {
+        constexpr int RING = 2 * TW + 2 * (TH + 2);  // 164
+        for (int q = tid; q < RING; q += NTH) {
+            int rx, ry2;
+            if (q < TW) { rx = HX + q; ry2 = 1; }
+            else if (q < 2 * TW) { rx = HX + q - TW; ry2 = TH + 2; }
+            else if (q < 2 * TW + TH + 2) { rx = HX - 1; ry2 = 1 + q - 2 * TW; }
+            else { rx = HX + TW; ry2 = 1 + q - 2 * TW - (TH + 2); }
+            float o8[8];
+            outflows_scalar<EDGE>(c, be, rx, ry2, gx0 + rx, gy0 + ry2, o8);
+            const int oi = (ry2 - 1) * RW + rx;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) outf[d * O_C + oi] = o8[d];
+        }
+    }
+    __syncthreads();
+    // ---- thermal_transport: own outflows out, neighbours' outflows in -------
+    {
+        const int oi = (ry - 1) * RW + rx0;
+        float4 own4[8];
+#pragma unroll
+        for (int d = 0; d < 8; ++d) own4[d] = ld4(outf + d * O_C + oi);
+        // inflow from direction d = neighbour (dx, dy)'s outflow opp(d)
+        const float4 inT = ld4(outf + 3 * O_C + oi + RW);  // top neighbour's B
+        const float4 inB = ld4(outf + 2 * O_C + oi - RW);  // bottom neighbour's T
+        const float4 b4 = ld4(be + ry * RW + rx0);
+        float res[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int o = oi + j;
             float own[8], in[8];
 #pragma unroll
-            for (int d = 0; d < 8; ++d) {
-                own[d] = outf[d * O_C + oi];
-                in[d] = outf[f_opp[d] * O_C + oi + f_oy[d] * O_W + f_ox[d]];
-            }
-            float b = be[(iy0 + 2) * T_RW + ix0 + HX];
-            a.out.f[S_ROCK][gi] = cell_thermal_apply(b, own, in);
+            for (int d = 0; d < 8; ++d) own[d] = at4(own4[d], j);
+            in[0] = outf[1 * O_C + o - 1];       // L neighbour's R
+            in[1] = outf[0 * O_C + o + 1];       // R neighbour's L
+            in[2] = at4(inT, j);                 // T neighbour's B
+            in[3] = at4(inB, j);                 // B neighbour's T
+            in[4] = outf[7 * O_C + o + RW - 1];  // LT neighbour's RB
+            in[5] = outf[6 * O_C + o + RW + 1];  // RT neighbour's LB
+            in[6] = outf[5 * O_C + o - RW - 1];  // LB neighbour's RT
+            in[7] = outf[4 * O_C + o - RW + 1];  // RB neighbour's LT
+            res[j] = cell_thermal_apply(at4(b4, j), own, in);
         }
+        *reinterpret_cast<float4*>(a.out.f[S_ROCK] + gi0) = make_float4(res[0], res[1], res[2], res[3]);
     }
 }
 
-__global__ void __launch_bounds__(NTH) k_transport(FusedArgs a) {
-    __shared__ __align__(16) float be[T_RC];
-    __shared__ float outf[8 * O_C];
+__global__ void __launch_bounds__(NTH) k_transport(const __grid_constant__ TmaMaps maps, const __grid_constant__ FusedArgs a) {
+    __shared__ __align__(128) float be[T_BOX];
+    __shared__ __align__(16) float outf[8 * O_C];
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
     const int n = a.c.n;
     const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 2 >= 0 && ty0 + TH + 2 <= n;
-    if (inner) transport_tile<false>(a, be, outf, tx0, ty0);
-    else transport_tile<true>(a, be, outf, tx0, ty0);
+    if (inner) transport_tile<false>(maps, a, be, outf, &bar, tx0, ty0);
+    else transport_tile<true>(maps, a, be, outf, &bar, tx0, ty0);
+}
+
+// ---------------------------------------------------------------------------
+// tensor maps
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+bool encode_box(CUtensorMap* map, const float* base, int n, int box_h) {
+    std::call_once(g_encode_once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    if (!g_encode) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+    cuuint64_t strides[1] = {(cuuint64_t)n * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)RW, (cuuint32_t)box_h};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
 }
 
 }  // namespace
+
+// Tensor maps are cached per buffer: a world's buffers live as long as it does.
+bool TmaCache::get(const float* base, int n, int box_h, CUtensorMap* out) {
+    for (auto& e : entries)
+        if (e.base == base && e.n == n && e.box_h == box_h) {
+            *out = e.map;
+            return true;
+        }
+    Entry e{base, n, box_h, {}};
+    if (!encode_box(&e.map, base, n, box_h)) return false;
+    entries.push_back(e);
+    *out = e.map;
+    return true;
+}
 
 int fused_max_depth() { return 1; }
 
 bool fused_supported(int depth, int tile_x, int tile_y) { return depth == 1 && tile_x == TW && tile_y == TH; }
 
-void launch_fused(const FusedArgs& a, int depth, int tile_x, int tile_y, cudaStream_t st) {
-    (void)depth; (void)tile_x; (void)tile_y;
+bool launch_fused(const FusedArgs& a, TmaCache& cache, cudaStream_t st) {
+    TmaMaps maps;
+    const int in_fields[H_N] = {S_ROCK, S_WATER, S_SED, S_FL, S_FR, S_FT, S_FB};
+    for (int f = 0; f < H_N; ++f)
+        if (!cache.get(a.in.f[in_fields[f]], a.c.n, H_RH, &maps.m[f])) return false;
+    if (!cache.get(a.b_ero, a.c.n, T_RH, &maps.m[H_N])) return false;
     dim3 grid(a.c.n / TW, a.c.n / TH);
-    k_hydro<<<grid, NTH, 0, st>>>(a);
-    k_transport<<<grid, NTH, 0, st>>>(a);
+    k_hydro<<<grid, NTH, 0, st>>>(maps, a);
+    k_transport<<<grid, NTH, 0, st>>>(maps, a);
     count_launch(2);
+    return true;
 }
 
 }  // namespace hg

@@ -1,9 +1,11 @@
 // Internal declarations shared by the library's translation units.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <atomic>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/hydrogen.h"
 #include "hg_device.cuh"
@@ -42,9 +44,29 @@ struct FusedArgs {
     float* v;
     float* s_ero;  // eroded sediment of every cell (k_hydro -> k_transport)
     float* b_ero;  // eroded rock of every cell (k_hydro -> k_transport, thermal on)
+    int* err;      // set to 1 when a bounded wait for a TMA tile gives up
 };
+
+// TMA tensor maps of the fused step: rock, water, sediment, fL, fR, fT, fB
+// (k_hydro boxes) and eroded rock (k_transport box).
+struct TmaMaps {
+    CUtensorMap m[8];
+};
+// Tensor maps encoded once per (buffer, box) and reused.
+struct TmaCache {
+    struct Entry {
+        const float* base;
+        int n, box_h;
+        CUtensorMap map;
+    };
+    std::vector<Entry> entries;
+    bool get(const float* base, int n, int box_h, CUtensorMap* out);
+};
+
 int fused_max_depth();
-void launch_fused(const FusedArgs& a, int depth, int tile_x, int tile_y, cudaStream_t st);
+// Launches k_hydro and k_transport for one step; false if a tensor map could
+// not be encoded.
+bool launch_fused(const FusedArgs& a, TmaCache& cache, cudaStream_t st);
 // The fused kernel's tile shape and depth currently compiled in.
 bool fused_supported(int depth, int tile_x, int tile_y);
 

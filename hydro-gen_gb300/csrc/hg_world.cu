@@ -73,6 +73,8 @@ struct hg_world {
     bool ks_on = false;
     float* s_ero = nullptr;  // fused step: eroded sediment of every cell
     float* b_ero = nullptr;  // fused step: eroded rock of every cell
+    int* err = nullptr;      // device flag: a bounded wait gave up
+    TmaCache tma;
     float* red_f = nullptr;   // min/max partials + result
     double* red_d = nullptr;  // FP64 partials + result
 };
@@ -123,7 +125,7 @@ void free_world(hg_world* w) {
     cudaFree(w->u); cudaFree(w->v); cudaFree(w->vz);
     cudaFree(w->tc); cudaFree(w->td);
     cudaFree(w->ks);
-    cudaFree(w->s_ero); cudaFree(w->b_ero);
+    cudaFree(w->s_ero); cudaFree(w->b_ero); cudaFree(w->err);
     cudaFree(w->red_f); cudaFree(w->red_d);
     if (w->stream) cudaStreamDestroy(w->stream);
 }
@@ -324,6 +326,8 @@ int hg_world_create(int n, int layers, hg_world** out) {
     if (e == cudaSuccess) e = alloc((void**)&w->ks, bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->s_ero, bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->b_ero, bytes);
+    if (e == cudaSuccess) e = alloc((void**)&w->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->err, 0, sizeof(int), w->stream);
     if (e == cudaSuccess) e = alloc((void**)&w->red_f, sizeof(float) * (2 * reduction_parts() + 2));
     if (e == cudaSuccess) e = alloc((void**)&w->red_d, sizeof(double) * (8 * reduction_parts() + 8));
     if (e != cudaSuccess) {
@@ -552,7 +556,9 @@ int hg_step(hg_world* w, int nsteps, int mode) {
             a.v = w->v;
             a.s_ero = w->s_ero;
             a.b_ero = w->b_ero;
-            launch_fused(a, 1, tx, ty, st);
+            a.err = w->err;
+            if (!launch_fused(a, w->tma, st))
+                return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a world buffer");
             for (int f = 0; f < S_COUNT; ++f) swap(f);
             w->step += 1;
         }
@@ -565,6 +571,13 @@ int hg_sync(hg_world* w) {
     HG_CHECK_WORLD(w);
     DeviceGuard g(w->device);
     HG_CUDA(cudaStreamSynchronize(w->stream));
+    int flag = 0;
+    HG_CUDA(cudaMemcpy(&flag, w->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        HG_CUDA(cudaMemset(w->err, 0, sizeof(int)));
+        return fail(HG_ERR_TIMEOUT, "a fused-step tile load did not arrive within its bounded wait; "
+                                    "the step's fields are not valid");
+    }
     return HG_OK;
 }
 
