@@ -14,17 +14,26 @@
 // intermediate traffic (eroded rock and sediment written and read once) and
 // saves recomputing flux and erosion on a halo ring.
 //
-// Both kernels work on 64 x 16 tiles with 256 threads; each thread owns a
-// row group of four horizontally adjacent cells, so neighbour values come
-// from float4 shared-memory rows and every HBM write is a float4.
-//   k_hydro stages rock, water and the four fluxes of the tile plus a halo
-//   (4 columns, 1 row) with six TMA 2-D tile loads; while they fly, threads
-//   draw this step's Philox rain words and load their own sediment; rain is
-//   then added in shared memory.
-//   k_transport stages the eroded rock with a 2-row halo by one TMA load,
-//   computes each cell's eight talus outflows once (the ring of interior
-//   plus 1 included) into shared memory, then applies outflow and inflow,
-//   and gathers the four sediment taps of every cell from HBM/L2.
+// Both kernels are table driven: one launch covers every 64 x TH tile of any
+// number of worlds ("terrains") of different sizes and settings.  A block
+// finds its terrain by binary search over the terrains' first tile indices
+// and reads the terrain's descriptor (TMA tensor maps, step constants, rain
+// settings, buffers, step counter) from global memory.  A single world is a
+// table of one terrain.  The rain step number comes from the terrain's device
+// step counter (advanced by k_transport), so a captured CUDA graph of a few
+// steps can be replayed any number of times.
+//
+//   k_hydro stages rock, water, sediment and the four fluxes of the tile plus
+//   a halo (4 columns, 1 row) with seven TMA 2-D tile loads; while they fly,
+//   threads draw this step's Philox rain words; rain is then added in shared
+//   memory.  Each thread computes TW*TH/NTH cells, one per iteration (low
+//   register use keeps ~6 blocks per SM to hide the long dependent chains of
+//   flux and erosion), a warp covering 32 consecutive cells of a row.
+//   k_transport stages the eroded rock with a 2-row halo by one TMA load;
+//   each thread owns a row group of four horizontally adjacent cells: it
+//   computes their eight talus outflows once into shared memory (the ring of
+//   interior plus 1 too), applies outflow and inflow, and gathers the four
+//   sediment taps of every cell from L2/HBM.
 //
 // Per-cell arithmetic is the code of the per-pass kernels (hg_device.cuh),
 // so the fused step reproduces them bit for bit.
@@ -40,55 +49,79 @@ namespace hg {
 
 namespace {
 
-constexpr int TW = 64, TH = 16, NTH = 256;
-constexpr int GPR = TW / 4;  // row groups per tile row (16)
-constexpr int HX = 4;        // halo columns: 16-byte aligned TMA boxes
+constexpr int TW = 64;
+constexpr int GPR = TW / 4;      // row groups per tile row (16)
+constexpr int HX = 4;            // halo columns: 16-byte aligned TMA boxes
 constexpr int RW = TW + 2 * HX;  // 72
-
-// k_hydro region: (TW + 8) x (TH + 2), origin (tx0 - 4, ty0 - 1)
-constexpr int H_RH = TH + 2, H_BOX = RW * H_RH;  // 1296 floats
-constexpr int H_RC = ((H_BOX + 31) / 32) * 32;   // 128-byte aligned array stride
 enum { H_B = 0, H_D, H_S, H_FL, H_FR, H_FT, H_FB, H_N };
+constexpr int M_BERO = H_N;      // tensor map index of the eroded rock
 
-// k_transport region: (TW + 8) x (TH + 4), origin (tx0 - 4, ty0 - 2)
-constexpr int T_RH = TH + 4, T_BOX = RW * T_RH;  // 1440 floats
-// outflows of interior plus 1: region rows 1..TH+2, same column layout
-constexpr int O_RH = TH + 2, O_C = RW * O_RH;    // 1296 floats per direction
+// Geometry of a 64 x TH tile: TH = 16 with 256 threads or TH = 8 with 128.
+template <int TH>
+struct Geo {
+    static constexpr int NTH = TH * GPR;                 // one row group per thread in k_transport
+    static constexpr int H_RH = TH + 2, H_BOX = RW * H_RH;
+    static constexpr int H_RC = ((H_BOX + 31) / 32) * 32;  // 128-byte aligned array stride
+    static constexpr int T_RH = TH + 4, T_BOX = RW * T_RH;
+    static constexpr int O_RH = TH + 2, O_C = RW * O_RH;   // outflows of interior plus 1
+    static constexpr int CPT = TW * TH / NTH;             // cells per thread in k_hydro (4)
+};
 
-// direction d: L, R, T, B, LT, RT, LB, RB; offsets and the opposite direction
+// direction d: L, R, T, B, LT, RT, LB, RB
 __constant__ int f_ox[8] = {-1, 1, 0, 0, -1, 1, -1, 1};
 __constant__ int f_oy[8] = {0, 0, 1, -1, 1, 1, -1, -1};
-__constant__ int f_opp[8] = {1, 0, 3, 2, 7, 6, 5, 4};
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float at4(const float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
 
-__device__ __forceinline__ void report_timeout(const FusedArgs& a) {
-    if (threadIdx.x == 0) atomicExch(a.err, 1);
+__device__ __forceinline__ int find_terrain(const int* __restrict__ tile0, int nterr, int tile) {
+    int lo = 0, hi = nterr - 1;
+    while (lo < hi) {  // last terrain whose first tile <= tile
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(tile0 + mid) <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ RainStep rain_for(const RainBase& rb, unsigned long long step1) {
+    RainStep r;
+    r.active = (rb.mode != 0 && rb.period > 0 && step1 % (unsigned long long)rb.period == 0ull) ? 1 : 0;
+    r.bernoulli = rb.mode == 2 ? 1 : 0;
+    r.amount = rb.amount;
+    r.threshold = rb.threshold;
+    r.seed_lo = rb.seed_lo;
+    r.seed_hi = rb.seed_hi;
+    r.terrain_id = rb.terrain_id;
+    r.step = (uint32_t)step1;
+    return r;
 }
 
 // ---------------------------------------------------------------------------
 // k_hydro
 // ---------------------------------------------------------------------------
-template <bool EDGE>
-__device__ __forceinline__ void hydro_tile(const TmaMaps& maps, const FusedArgs& a, float* sm, uint64_t* bar,
-                                           int tx0, int ty0) {
-    const StepConsts& c = a.c;
-    const RainStep& r = a.rain[0];
+template <int TH, bool EDGE>
+__device__ __forceinline__ void hydro_tile(const TerrainDesc& td, float* sm, uint64_t* bar, int tx0, int ty0,
+                                           int* err) {
+    using G = Geo<TH>;
+    constexpr int NTH = G::NTH, H_RC = G::H_RC, H_RH = G::H_RH;
+    const StepConsts& c = td.c;
+    const RainStep r = rain_for(td.rain, *td.step + 1ull);
     const int n = c.n;
     const int tid = threadIdx.x;
     const int gx0 = tx0 - HX, gy0 = ty0 - 1;
     if (tid == 0) {
-        mbar_arrive_expect_tx(bar, H_N * H_BOX * sizeof(float));
+        mbar_arrive_expect_tx(bar, H_N * G::H_BOX * sizeof(float));
 #pragma unroll
-        for (int f = 0; f < H_N; ++f) tma_load_2d(sm + f * H_RC, &maps.m[f], gx0, gy0, bar);
+        for (int f = 0; f < H_N; ++f) tma_load_2d(sm + f * H_RC, &td.maps[f], gx0, gy0, bar);
     }
-    // rain words of the region's row groups (18 rows x 18 groups), drawn while the tiles load
-    constexpr int RG = (RW / 4) * H_RH;  // 324
-    uint32_t words[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+    // rain words of the region's row groups, drawn while the tiles load
+    constexpr int RG = (RW / 4) * H_RH;
+    constexpr int RGK = (RG + NTH - 1) / NTH;
+    uint32_t words[RGK][4];
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < RGK; ++k) {
+        words[k][0] = words[k][1] = words[k][2] = words[k][3] = 0;
         int q = tid + k * NTH;
         if (q < RG && r.active && r.bernoulli) {
             int gx = gx0 + (q % (RW / 4)) * 4, gy = gy0 + q / (RW / 4);
@@ -97,14 +130,14 @@ __device__ __forceinline__ void hydro_tile(const TmaMaps& maps, const FusedArgs&
     }
     bool ok = __syncthreads_and(mbar_wait(bar, 0));
     if (!ok) {  // the tile never arrived: record, give the copies one more bounded wait, skip the tile
-        report_timeout(a);
+        if (tid == 0) atomicExch(err, 1);
         mbar_wait(bar, 0);
         return;
     }
     if (r.active) {
         float* D = sm + H_D * H_RC;
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < RGK; ++k) {
             int q = tid + k * NTH;
             if (q >= RG) continue;
             int rx = (q % (RW / 4)) * 4, ry = q / (RW / 4);
@@ -127,11 +160,8 @@ __device__ __forceinline__ void hydro_tile(const TmaMaps& maps, const FusedArgs&
     const float* FR = sm + H_FR * H_RC;
     const float* FT = sm + H_FT * H_RC;
     const float* FB = sm + H_FB * H_RC;
-    // one cell per iteration (low register use keeps ~5 blocks per SM to hide
-    // the long dependent chains of flux and erosion); a warp covers 32
-    // consecutive cells of a row
 #pragma unroll 1
-    for (int k = 0; k < TW * TH / NTH; ++k) {
+    for (int k = 0; k < G::CPT; ++k) {
         const int q = tid + k * NTH;
         const int ix = q % TW, iy = q / TW;
         const int x = tx0 + ix, y = ty0 + iy;
@@ -156,28 +186,45 @@ __device__ __forceinline__ void hydro_tile(const TmaMaps& maps, const FusedArgs&
         float Kls0 = c.ks_field ? c.dt * __ldg(c.ks_field + gi) : c.Kls0;
         cell_erosion(c, Kls0, o.u, o.v, o.vz, b, s, has_r ? br : 0.0f, has_l ? bl : 0.0f, has_b ? bb : 0.0f,
                      has_t ? bt : 0.0f);
-        a.out.f[S_FL][gi] = o.fl;
-        a.out.f[S_FR][gi] = o.fr;
-        a.out.f[S_FT][gi] = o.ft;
-        a.out.f[S_FB][gi] = o.fb;
-        a.out.f[S_WATER][gi] = o.d2 * c.evap;  // sediment_transport's evaporation (glsl/sediment_transport.glsl:75)
-        a.u[gi] = o.u;
-        a.v[gi] = o.v;
-        a.s_ero[gi] = s;
-        (c.thermal ? a.b_ero : a.out.f[S_ROCK])[gi] = b;  // no thermal pass: eroded rock is final
+        td.out[S_FL][gi] = o.fl;
+        td.out[S_FR][gi] = o.fr;
+        td.out[S_FT][gi] = o.ft;
+        td.out[S_FB][gi] = o.fb;
+        td.out[S_WATER][gi] = o.d2 * c.evap;  // sediment_transport's evaporation (glsl/sediment_transport.glsl:75)
+        td.u[gi] = o.u;
+        td.v[gi] = o.v;
+        td.s_ero[gi] = s;
+        (c.thermal ? td.b_ero : td.out[S_ROCK])[gi] = b;  // no thermal pass: eroded rock is final
     }
 }
 
-__global__ void __launch_bounds__(NTH) k_hydro(const __grid_constant__ TmaMaps maps, const __grid_constant__ FusedArgs a) {
-    __shared__ __align__(128) float sm[H_N * H_RC];
+template <int TH>
+__device__ __forceinline__ void hydro_block(const TerrainDesc& td, int tile, int* err) {
+    using G = Geo<TH>;
+    __shared__ __align__(128) float sm[H_N * G::H_RC];
     __shared__ __align__(8) uint64_t bar;
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
-    const int n = a.c.n;
-    const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+    const int n = td.c.n;
+    const int tx0 = (tile % td.tiles_x) * TW, ty0 = (tile / td.tiles_x) * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 1 >= 0 && ty0 + TH + 1 <= n;
-    if (inner) hydro_tile<false>(maps, a, sm, &bar, tx0, ty0);
-    else hydro_tile<true>(maps, a, sm, &bar, tx0, ty0);
+    if (inner) hydro_tile<TH, false>(td, sm, &bar, tx0, ty0, err);
+    else hydro_tile<TH, true>(td, sm, &bar, tx0, ty0, err);
+}
+
+// Batch form: descriptors in global memory, the block finds its terrain.
+template <int TH>
+__global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro(const TerrainDesc* __restrict__ tds,
+                                                        const int* __restrict__ tile0, int nterr, int* err) {
+    const int t = find_terrain(tile0, nterr, blockIdx.x);
+    hydro_block<TH>(tds[t], blockIdx.x - __ldg(tile0 + t), err);
+}
+
+// Single-world form: the descriptor is a kernel parameter, so the step
+// constants are read from the constant bank.
+template <int TH>
+__global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro1(const __grid_constant__ TerrainDesc td, int* err) {
+    hydro_block<TH>(td, blockIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -212,22 +259,24 @@ __device__ __forceinline__ void outflows_scalar(const StepConsts& c, const float
     for (int d = 0; d < 8; ++d) o8[d] = (t.mask >> d & 1u) ? t.S * (b - nb[d]) / t.bk : 0.0f;
 }
 
-template <bool EDGE>
-__device__ __forceinline__ void transport_tile(const TmaMaps& maps, const FusedArgs& a, float* be, float* outf,
-                                               uint64_t* bar, int tx0, int ty0) {
-    const StepConsts& c = a.c;
+template <int TH, bool EDGE>
+__device__ __forceinline__ void transport_tile(const TerrainDesc& td, float* be, float* outf, uint64_t* bar,
+                                               int tx0, int ty0, int* err) {
+    using G = Geo<TH>;
+    constexpr int NTH = G::NTH, O_C = G::O_C;
+    const StepConsts& c = td.c;
     const int n = c.n;
     const int tid = threadIdx.x;
     const int gx0 = tx0 - HX, gy0 = ty0 - 2;
     if (c.thermal && tid == 0) {
-        mbar_arrive_expect_tx(bar, T_BOX * sizeof(float));
-        tma_load_2d(be, &maps.m[H_N], gx0, gy0, bar);
+        mbar_arrive_expect_tx(bar, G::T_BOX * sizeof(float));
+        tma_load_2d(be, &td.maps[M_BERO], gx0, gy0, bar);
     }
     const int iy = tid / GPR, g = tid % GPR;
     const int x0 = tx0 + 4 * g, y = ty0 + iy;
     const size_t gi0 = (size_t)y * n + x0;
-    const float4 u4 = __ldg(reinterpret_cast<const float4*>(a.u + gi0));
-    const float4 v4 = __ldg(reinterpret_cast<const float4*>(a.v + gi0));
+    const float4 u4 = __ldg(reinterpret_cast<const float4*>(td.u + gi0));
+    const float4 v4 = __ldg(reinterpret_cast<const float4*>(td.v + gi0));
 
     // sediment_transport: semi-Lagrangian gather of eroded sediment (any reach)
     float sed[4];
@@ -236,19 +285,19 @@ __device__ __forceinline__ void transport_tile(const TmaMaps& maps, const FusedA
         float px, py;
         backtrace(c, x0 + j, y, at4(u4, j), at4(v4, j), px, py);
         int ix = min(max((int)px, 0), n - 1), iy2 = min(max((int)py, 0), n - 1);
-        const float* se = a.s_ero + (size_t)iy2 * n + ix;
+        const float* se = td.s_ero + (size_t)iy2 * n + ix;
         float s00 = __ldg(se);
         float s10 = ix + 1 < n ? __ldg(se + 1) : 0.0f;
         float s01 = iy2 + 1 < n ? __ldg(se + n) : 0.0f;
         float s11 = (ix + 1 < n && iy2 + 1 < n) ? __ldg(se + n + 1) : 0.0f;
         sed[j] = bilinear_mix(px, py, s00, s10, s01, s11);
     }
-    *reinterpret_cast<float4*>(a.out.f[S_SED] + gi0) = make_float4(sed[0], sed[1], sed[2], sed[3]);
+    st4(td.out[S_SED] + gi0, make_float4(sed[0], sed[1], sed[2], sed[3]));
     if (!c.thermal) return;
 
     bool ok = __syncthreads_and(mbar_wait(bar, 0));
     if (!ok) {
-        report_timeout(a);
+        if (tid == 0) atomicExch(err, 1);
         mbar_wait(bar, 0);
         return;
     }
@@ -286,7 +335,7 @@ __device__ __forceinline__ void transport_tile(const TmaMaps& maps, const FusedA
     }
     // ---- outflows of the ring of interior plus 1 ---------------------------
     {
-        constexpr int RING = 2 * TW + 2 * (TH + 2);  // 164
+        constexpr int RING = 2 * TW + 2 * (TH + 2);
         for (int q = tid; q < RING; q += NTH) {
             int rx, ry2;
             if (q < TW) { rx = HX + q; ry2 = 1; }
@@ -307,7 +356,7 @@ __device__ __forceinline__ void transport_tile(const TmaMaps& maps, const FusedA
         float4 own4[8];
 #pragma unroll
         for (int d = 0; d < 8; ++d) own4[d] = ld4(outf + d * O_C + oi);
-        // inflow from direction d = neighbour (dx, dy)'s outflow opp(d)
+        // inflow from direction d = neighbour (dx, dy)'s outflow toward this cell
         const float4 inT = ld4(outf + 3 * O_C + oi + RW);  // top neighbour's B
         const float4 inB = ld4(outf + 2 * O_C + oi - RW);  // bottom neighbour's T
         const float4 b4 = ld4(be + ry * RW + rx0);
@@ -328,21 +377,38 @@ __device__ __forceinline__ void transport_tile(const TmaMaps& maps, const FusedA
             in[7] = outf[4 * O_C + o - RW + 1];  // RB neighbour's LT
             res[j] = cell_thermal_apply(at4(b4, j), own, in);
         }
-        *reinterpret_cast<float4*>(a.out.f[S_ROCK] + gi0) = make_float4(res[0], res[1], res[2], res[3]);
+        st4(td.out[S_ROCK] + gi0, make_float4(res[0], res[1], res[2], res[3]));
     }
 }
 
-__global__ void __launch_bounds__(NTH) k_transport(const __grid_constant__ TmaMaps maps, const __grid_constant__ FusedArgs a) {
-    __shared__ __align__(128) float be[T_BOX];
-    __shared__ __align__(16) float outf[8 * O_C];
+template <int TH>
+__device__ __forceinline__ void transport_block(const TerrainDesc& td, int tile, int* err) {
+    using G = Geo<TH>;
+    __shared__ __align__(128) float be[G::T_BOX];
+    __shared__ __align__(16) float outf[8 * G::O_C];
     __shared__ __align__(8) uint64_t bar;
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
-    const int n = a.c.n;
-    const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * TH;
+    const int n = td.c.n;
+    const int tx0 = (tile % td.tiles_x) * TW, ty0 = (tile / td.tiles_x) * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 2 >= 0 && ty0 + TH + 2 <= n;
-    if (inner) transport_tile<false>(maps, a, be, outf, &bar, tx0, ty0);
-    else transport_tile<true>(maps, a, be, outf, &bar, tx0, ty0);
+    if (inner) transport_tile<TH, false>(td, be, outf, &bar, tx0, ty0, err);
+    else transport_tile<TH, true>(td, be, outf, &bar, tx0, ty0, err);
+    // k_hydro of this step has finished (stream order) and the next step's
+    // k_hydro starts after this launch: advance the terrain's step counter
+    if (tile == 0 && threadIdx.x == 0) *td.step += 1ull;
+}
+
+template <int TH>
+__global__ void __launch_bounds__(Geo<TH>::NTH) k_transport(const TerrainDesc* __restrict__ tds,
+                                                            const int* __restrict__ tile0, int nterr, int* err) {
+    const int t = find_terrain(tile0, nterr, blockIdx.x);
+    transport_block<TH>(tds[t], blockIdx.x - __ldg(tile0 + t), err);
+}
+
+template <int TH>
+__global__ void __launch_bounds__(Geo<TH>::NTH) k_transport1(const __grid_constant__ TerrainDesc td, int* err) {
+    transport_block<TH>(td, blockIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -373,7 +439,6 @@ bool encode_box(CUtensorMap* map, const float* base, int n, int box_h) {
 
 }  // namespace
 
-// Tensor maps are cached per buffer: a world's buffers live as long as it does.
 bool TmaCache::get(const float* base, int n, int box_h, CUtensorMap* out) {
     for (auto& e : entries)
         if (e.base == base && e.n == n && e.box_h == box_h) {
@@ -387,21 +452,49 @@ bool TmaCache::get(const float* base, int n, int box_h, CUtensorMap* out) {
     return true;
 }
 
-int fused_max_depth() { return 1; }
+bool fused_tile_ok(int n, int th) { return (th == 16 || th == 8) && n % TW == 0 && n % th == 0; }
 
-bool fused_supported(int depth, int tile_x, int tile_y) { return depth == 1 && tile_x == TW && tile_y == TH; }
+int fused_tiles(int n, int th) { return (n / TW) * (n / th); }
 
-bool launch_fused(const FusedArgs& a, TmaCache& cache, cudaStream_t st) {
-    TmaMaps maps;
+bool fill_desc(TerrainDesc& d, const TerrainSrc& s, int th, int tile0, TmaCache& cache) {
+    d.c = s.c;
+    d.rain = s.rain;
+    for (int f = 0; f < S_COUNT; ++f) d.out[f] = s.out[f];
+    d.u = s.u;
+    d.v = s.v;
+    d.s_ero = s.s_ero;
+    d.b_ero = s.b_ero;
+    d.step = s.step;
+    d.tiles_x = s.c.n / TW;
+    d.tile0 = tile0;
     const int in_fields[H_N] = {S_ROCK, S_WATER, S_SED, S_FL, S_FR, S_FT, S_FB};
     for (int f = 0; f < H_N; ++f)
-        if (!cache.get(a.in.f[in_fields[f]], a.c.n, H_RH, &maps.m[f])) return false;
-    if (!cache.get(a.b_ero, a.c.n, T_RH, &maps.m[H_N])) return false;
-    dim3 grid(a.c.n / TW, a.c.n / TH);
-    k_hydro<<<grid, NTH, 0, st>>>(maps, a);
-    k_transport<<<grid, NTH, 0, st>>>(maps, a);
+        if (!cache.get(s.in[in_fields[f]], s.c.n, th + 2, &d.maps[f])) return false;
+    return cache.get(s.b_ero, s.c.n, th + 4, &d.maps[M_BERO]);
+}
+
+void launch_fused_table(const TerrainDesc* tds, const int* tile0, int nterr, int total_tiles, int th, int* err,
+                        cudaStream_t st) {
+    if (th == 16) {
+        k_hydro<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(tds, tile0, nterr, err);
+        k_transport<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(tds, tile0, nterr, err);
+    } else {
+        k_hydro<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(tds, tile0, nterr, err);
+        k_transport<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(tds, tile0, nterr, err);
+    }
     count_launch(2);
-    return true;
+}
+
+void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st) {
+    const int tiles = fused_tiles(td.c.n, th);
+    if (th == 16) {
+        k_hydro1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);
+        k_transport1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);
+    } else {
+        k_hydro1<8><<<tiles, Geo<8>::NTH, 0, st>>>(td, err);
+        k_transport1<8><<<tiles, Geo<8>::NTH, 0, st>>>(td, err);
+    }
+    count_launch(2);
 }
 
 }  // namespace hg

@@ -36,22 +36,45 @@ void launch_thermal_in(const StepConsts& c, const float* rock, const float4* tc,
                        float* rock_o, cudaStream_t st);
 
 // ---- fused step (hg_fused.cu) ---------------------------------------------------
-struct FusedArgs {
+// Rain settings without the step number (the kernels add the step).
+struct RainBase {
+    int mode;  // HG_RAIN_*
+    int period;
+    float amount;
+    uint32_t threshold;
+    uint32_t seed_lo, seed_hi, terrain_id;
+};
+
+// One terrain (world) of a fused launch, as the kernels read it from global
+// memory.  maps[0..6]: TMA boxes of the step's input rock, water, sediment,
+// fL, fR, fT, fB; maps[7]: eroded rock.  (CUtensorMap makes it 64-byte aligned.)
+struct TerrainDesc {
+    CUtensorMap maps[8];
     StepConsts c;
-    RainStep rain[8];  // per sub-step
-    StateBufs in, out;
+    RainBase rain;
+    float* out[S_COUNT];
     float* u;
     float* v;
     float* s_ero;  // eroded sediment of every cell (k_hydro -> k_transport)
     float* b_ero;  // eroded rock of every cell (k_hydro -> k_transport, thermal on)
-    int* err;      // set to 1 when a bounded wait for a TMA tile gives up
+    unsigned long long* step;  // device step counter (steps completed)
+    int tiles_x;
+    int tile0;  // first tile of this terrain in the launch
 };
 
-// TMA tensor maps of the fused step: rock, water, sediment, fL, fR, fT, fB
-// (k_hydro boxes) and eroded rock (k_transport box).
-struct TmaMaps {
-    CUtensorMap m[8];
+// Host view of one terrain for one step direction (inputs -> outputs).
+struct TerrainSrc {
+    StepConsts c;
+    RainBase rain;
+    const float* in[S_COUNT];
+    float* out[S_COUNT];
+    float* u;
+    float* v;
+    float* s_ero;
+    float* b_ero;
+    unsigned long long* step;
 };
+
 // Tensor maps encoded once per (buffer, box) and reused.
 struct TmaCache {
     struct Entry {
@@ -63,12 +86,16 @@ struct TmaCache {
     bool get(const float* base, int n, int box_h, CUtensorMap* out);
 };
 
-int fused_max_depth();
-// Launches k_hydro and k_transport for one step; false if a tensor map could
-// not be encoded.
-bool launch_fused(const FusedArgs& a, TmaCache& cache, cudaStream_t st);
-// The fused kernel's tile shape and depth currently compiled in.
-bool fused_supported(int depth, int tile_x, int tile_y);
+// Tile height th (16 or 8) divides n and 64 divides n.
+bool fused_tile_ok(int n, int th);
+int fused_tiles(int n, int th);
+// Fills a descriptor (tensor maps from the cache); false if a map cannot be encoded.
+bool fill_desc(TerrainDesc& d, const TerrainSrc& s, int th, int tile0, TmaCache& cache);
+// k_hydro then k_transport over every tile of the table's terrains.
+void launch_fused_table(const TerrainDesc* tds, const int* tile0, int nterr, int total_tiles, int th, int* err,
+                        cudaStream_t st);
+// Same for one terrain whose descriptor travels as a kernel parameter.
+void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st);
 
 // ---- init and reductions (hg_init.cu) ---------------------------------------------
 void launch_fbm_raw(float* out, int n, const hg_noise_settings& s, cudaStream_t st);

@@ -8,7 +8,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <array>
 #include <new>
+#include <vector>
 #include <string>
 
 #include "hg_internal.h"
@@ -49,6 +51,16 @@ float host_poly_atanf(float x) {
     }
     return std::copysign((float)r, x);
 }
+
+struct Plan;
+
+// Fused-step variant chosen by the autotuner: tile height (16 or 8) and
+// whether steps replay a captured two-step CUDA graph.
+struct Tuning {
+    int th = 0;  // 0: not tuned yet
+    int graph = 0;
+    double ms[4] = {};  // ms per step of (16, direct), (16, graph), (8, direct), (8, graph)
+};
 }  // namespace hg
 
 using namespace hg;
@@ -74,10 +86,55 @@ struct hg_world {
     float* s_ero = nullptr;  // fused step: eroded sediment of every cell
     float* b_ero = nullptr;  // fused step: eroded rock of every cell
     int* err = nullptr;      // device flag: a bounded wait gave up
+    unsigned long long* d_step = nullptr;  // device copy of `step`, advanced by the fused kernels
+    bool dev_step_valid = false;           // d_step == step
+    uint64_t version = 1;                  // bumps whenever settings, options or Ks change
     TmaCache tma;
+    hg::Plan* plans[2] = {};               // fused plans of this world alone, tile height 16 / 8
+    hg::Tuning tuning;                     // autotuned fused-step variant
     float* red_f = nullptr;   // min/max partials + result
     double* red_d = nullptr;  // FP64 partials + result
 };
+
+struct hg_batch {
+    std::vector<hg_world*> worlds;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr;
+    int* err = nullptr;
+    hg::Plan* plans[2] = {};
+    hg::Tuning tuning;
+};
+
+namespace hg {
+// A fused launch plan over one or more worlds: two descriptor tables in
+// device memory (step direction cur -> alt and alt -> cur as of the build),
+// the terrains' first tile indices, and lazily captured two-step graphs.
+struct Plan {
+    std::vector<hg_world*> worlds;
+    int th = 16;
+    int total = 0;  // tiles over all terrains
+    TerrainDesc* d_tab[2] = {};
+    std::vector<TerrainDesc> h_tab[2];  // host copies (a single world launches from these)
+    int* d_tile0 = nullptr;
+    std::vector<std::array<const float*, S_COUNT>> key_cur, key_alt;  // buffers at build time
+    std::vector<uint64_t> versions;
+    cudaGraphExec_t graph[2] = {};  // two steps starting with table 0 / table 1
+    cudaStream_t stream = nullptr;
+    int* err = nullptr;
+};
+
+void destroy_plan(Plan*& p) {
+    if (!p) return;
+    for (auto& g : p->graph)
+        if (g) cudaGraphExecDestroy(g);
+    cudaFree(p->d_tab[0]);
+    cudaFree(p->d_tab[1]);
+    cudaFree(p->d_tile0);
+    delete p;
+    p = nullptr;
+}
+}  // namespace hg
 
 namespace {
 
@@ -125,7 +182,8 @@ void free_world(hg_world* w) {
     cudaFree(w->u); cudaFree(w->v); cudaFree(w->vz);
     cudaFree(w->tc); cudaFree(w->td);
     cudaFree(w->ks);
-    cudaFree(w->s_ero); cudaFree(w->b_ero); cudaFree(w->err);
+    cudaFree(w->s_ero); cudaFree(w->b_ero); cudaFree(w->err); cudaFree(w->d_step);
+    for (Plan*& p : w->plans) destroy_plan(p);
     cudaFree(w->red_f); cudaFree(w->red_d);
     if (w->stream) cudaStreamDestroy(w->stream);
 }
@@ -219,15 +277,210 @@ RainStep make_rain(const hg_world* w, uint64_t step1) {
     return r;
 }
 
-bool pick_tile(const hg_world* w, int& tx, int& ty) {
-    const int cand[][2] = {{64, 16}};
-    if (w->opt.tile_x > 0 && w->opt.tile_y > 0) {
-        tx = w->opt.tile_x; ty = w->opt.tile_y;
-        return fused_supported(1, tx, ty) && w->n % tx == 0 && w->n % ty == 0;
+RainBase make_rain_base(const hg_world* w) {
+    RainStep r = make_rain(w, 1);
+    RainBase b{};
+    b.mode = w->opt.rain_mode;
+    b.period = w->rs.period;
+    b.amount = r.amount;
+    b.threshold = r.threshold;
+    b.seed_lo = r.seed_lo;
+    b.seed_hi = r.seed_hi;
+    b.terrain_id = r.terrain_id;
+    return b;
+}
+
+__global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+
+// Fills both descriptor tables of a plan from its worlds' current buffers
+// (table 0 steps cur -> alt, table 1 alt -> cur) and records the build state.
+int build_plan(Plan* p) {
+    const size_t nt = p->worlds.size();
+    for (auto& g : p->graph)  // captured launches hold the old descriptors
+        if (g) {
+            cudaStreamSynchronize(p->stream);
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    std::vector<int> tile0(nt);
+    p->total = 0;
+    for (size_t i = 0; i < nt; ++i) {
+        tile0[i] = p->total;
+        p->total += fused_tiles(p->worlds[i]->n, p->th);
     }
-    for (auto& cxy : cand)
-        if (w->n % cxy[0] == 0 && w->n % cxy[1] == 0) { tx = cxy[0]; ty = cxy[1]; return true; }
-    return false;
+    std::vector<TerrainDesc> tab(nt);
+    for (int dir = 0; dir < 2; ++dir) {
+        for (size_t i = 0; i < nt; ++i) {
+            hg_world* w = p->worlds[i];
+            TerrainSrc s{};
+            s.c = make_consts(w);
+            s.rain = make_rain_base(w);
+            for (int f = 0; f < S_COUNT; ++f) {
+                s.in[f] = dir == 0 ? w->cur[f] : w->alt[f];
+                s.out[f] = dir == 0 ? w->alt[f] : w->cur[f];
+            }
+            s.u = w->u;
+            s.v = w->v;
+            s.s_ero = w->s_ero;
+            s.b_ero = w->b_ero;
+            s.step = w->d_step;
+            if (!fill_desc(tab[i], s, p->th, tile0[i], w->tma))
+                return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a world buffer");
+        }
+        if (!p->d_tab[dir]) HG_CUDA(cudaMalloc((void**)&p->d_tab[dir], sizeof(TerrainDesc) * nt));
+        HG_CUDA(cudaMemcpyAsync(p->d_tab[dir], tab.data(), sizeof(TerrainDesc) * nt, cudaMemcpyHostToDevice,
+                                p->stream));
+        HG_CUDA(cudaStreamSynchronize(p->stream));  // `tab` is reused for the other direction
+        p->h_tab[dir] = tab;
+    }
+    if (!p->d_tile0) HG_CUDA(cudaMalloc((void**)&p->d_tile0, sizeof(int) * nt));
+    HG_CUDA(cudaMemcpyAsync(p->d_tile0, tile0.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, p->stream));
+    HG_CUDA(cudaStreamSynchronize(p->stream));
+    p->key_cur.resize(nt);
+    p->key_alt.resize(nt);
+    p->versions.resize(nt);
+    for (size_t i = 0; i < nt; ++i) {
+        for (int f = 0; f < S_COUNT; ++f) {
+            p->key_cur[i][f] = p->worlds[i]->cur[f];
+            p->key_alt[i][f] = p->worlds[i]->alt[f];
+        }
+        p->versions[i] = p->worlds[i]->version;
+    }
+    return HG_OK;
+}
+
+// Direction (table) of the next step: 0 if every world's current buffers are
+// the build's cur, 1 if they are the build's alt, -1 if the plan is stale
+// (settings changed, or per-pass steps swapped fields individually).
+int plan_dir(const Plan* p) {
+    if (p->key_cur.size() != p->worlds.size()) return -1;
+    int dir = -1;
+    for (size_t i = 0; i < p->worlds.size(); ++i) {
+        const hg_world* w = p->worlds[i];
+        if (w->version != p->versions[i]) return -1;
+        bool is_cur = true, is_alt = true;
+        for (int f = 0; f < S_COUNT; ++f) {
+            is_cur = is_cur && w->cur[f] == p->key_cur[i][f];
+            is_alt = is_alt && w->cur[f] == p->key_alt[i][f];
+        }
+        int d = is_cur ? 0 : is_alt ? 1 : -1;
+        if (d < 0 || (dir >= 0 && d != dir)) return -1;
+        dir = d;
+    }
+    return dir;
+}
+
+// One fused step in direction `dir`: a single world takes its descriptor as
+// a kernel parameter, a batch launches over the device table.
+void launch_dir(Plan* p, int dir) {
+    if (p->worlds.size() == 1) launch_fused_one(p->h_tab[dir][0], p->th, p->err, p->stream);
+    else launch_fused_table(p->d_tab[dir], p->d_tile0, (int)p->worlds.size(), p->total, p->th, p->err, p->stream);
+}
+
+// Brings a plan up to date (tables, device step counters, the graph that
+// starts with the next direction) without running a step; *dir gets the
+// next direction.
+int prepare_plan(Plan* p, bool use_graph, int* dir_out) {
+    int dir = plan_dir(p);
+    if (dir < 0) {
+        int rc = build_plan(p);
+        if (rc != HG_OK) return rc;
+        dir = 0;
+    }
+    for (hg_world* w : p->worlds)
+        if (!w->dev_step_valid) {
+            k_set_u64<<<1, 1, 0, p->stream>>>(w->d_step, (unsigned long long)w->step);
+            w->dev_step_valid = true;
+        }
+    const int nt = (int)p->worlds.size();
+    if (use_graph && !p->graph[dir]) {
+        cudaGraph_t g = nullptr;
+        HG_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+        launch_dir(p, dir);
+        launch_dir(p, 1 - dir);
+        cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+        g_launches.fetch_sub(4);  // captured, not run
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&p->graph[dir], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    *dir_out = dir;
+    return HG_OK;
+}
+
+// Runs nsteps fused steps of a plan's worlds on the plan's stream.
+int run_plan(Plan* p, int nsteps, bool use_graph) {
+    int dir = 0;
+    int rc = prepare_plan(p, use_graph && nsteps >= 2, &dir);
+    if (rc != HG_OK) return rc;
+    const int nt = (int)p->worlds.size();
+    int k = 0;
+    if (use_graph && nsteps >= 2) {
+        for (; k + 2 <= nsteps; k += 2) {
+            HG_CUDA(cudaGraphLaunch(p->graph[dir], p->stream));
+            count_launch(4);
+        }
+    }
+    for (; k < nsteps; ++k)
+        launch_dir(p, (dir + k) & 1);
+    HG_CUDA(cudaGetLastError());
+    for (hg_world* w : p->worlds) {
+        w->step += (uint64_t)nsteps;
+        if (nsteps & 1)
+            for (int f = 0; f < S_COUNT; ++f) std::swap(w->cur[f], w->alt[f]);
+    }
+    return HG_OK;
+}
+
+// Fused steps over `worlds` with the autotuned (or requested) variant.  The
+// first call with at least 8 steps and no tuned choice times two steps of
+// each variant (tile height 16/8 x direct launches/graph replay); every
+// variant gives identical fields, so tuning steps are ordinary steps.
+int fused_run(Plan** plans, const std::vector<hg_world*>& worlds, Tuning& tune, int req_th, int req_graph,
+              cudaStream_t st, int* err, int nsteps) {
+    for (hg_world* w : worlds)
+        if (!fused_tile_ok(w->n, 16)) return fail(HG_ERR_UNSUPPORTED, "fused mode needs n divisible by 64");
+    if (req_th != HG_AUTO && req_th != 16 && req_th != 8)
+        return fail(HG_ERR_UNSUPPORTED, "fused tile height must be 16 or 8");
+    auto plan_for = [&](int th) -> Plan* {
+        Plan*& p = plans[th == 16 ? 0 : 1];
+        if (!p) {
+            p = new Plan();
+            p->worlds = worlds;
+            p->th = th;
+            p->stream = st;
+            p->err = err;
+        }
+        return p;
+    };
+    if (req_th == HG_AUTO && req_graph == HG_AUTO && tune.th == 0 && nsteps >= 8) {
+        cudaEvent_t e0, e1;
+        HG_CUDA(cudaEventCreate(&e0));
+        HG_CUDA(cudaEventCreate(&e1));
+        double best = 1e30;
+        for (int cand = 0; cand < 4; ++cand) {
+            int th = cand < 2 ? 16 : 8, graph = cand & 1;
+            int dir = 0;
+            int rc0 = prepare_plan(plan_for(th), graph != 0, &dir);  // host work outside the timed span
+            if (rc0 != HG_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc0; }
+            cudaEventRecord(e0, st);
+            int rc = run_plan(plan_for(th), 2, graph != 0);
+            cudaEventRecord(e1, st);
+            if (rc != HG_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+            HG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            tune.ms[cand] = ms / 2.0;
+            if (tune.ms[cand] < best) { best = tune.ms[cand]; tune.th = th; tune.graph = graph; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        nsteps -= 8;
+    }
+    int th = req_th != HG_AUTO ? req_th : (tune.th ? tune.th : 16);
+    int graph = req_graph != HG_AUTO ? req_graph : (tune.th ? tune.graph : 1);
+    return run_plan(plan_for(th), nsteps, graph != 0);
 }
 
 float* field_ptr(hg_world* w, int field) {
@@ -290,7 +543,7 @@ int hg_default_step_options(hg_step_options* out) {
     std::memset(out, 0, sizeof(*out));
     out->rain_mode = HG_RAIN_OFF;
     out->thermal = HG_AUTO;
-    out->temporal_depth = HG_AUTO;
+    out->graph = HG_AUTO;
     out->tile_x = HG_AUTO;
     out->tile_y = HG_AUTO;
     return HG_OK;
@@ -327,6 +580,7 @@ int hg_world_create(int n, int layers, hg_world** out) {
     if (e == cudaSuccess) e = alloc((void**)&w->s_ero, bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->b_ero, bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->err, sizeof(int));
+    if (e == cudaSuccess) e = alloc((void**)&w->d_step, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemsetAsync(w->err, 0, sizeof(int), w->stream);
     if (e == cudaSuccess) e = alloc((void**)&w->red_f, sizeof(float) * (2 * reduction_parts() + 2));
     if (e == cudaSuccess) e = alloc((void**)&w->red_d, sizeof(double) * (8 * reduction_parts() + 8));
@@ -387,6 +641,7 @@ int hg_set_erosion_settings(hg_world* w, const hg_erosion_settings* s) {
     if (w->layers == 1 && s->Kspeed[1] != 0.0f)
         return fail(HG_ERR_INVALID, "Kspeed[1] must be 0 in a one-layer world (dirt slippage and smoothing)");
     w->es = *s;
+    w->version += 1;
     return HG_OK;
 }
 
@@ -402,6 +657,7 @@ int hg_set_rain_settings(hg_world* w, const hg_rain_settings* s) {
     if (!s) return fail(HG_ERR_INVALID, "null settings");
     if (s->period < 0) return fail(HG_ERR_INVALID, "rain period must be >= 0");
     w->rs = *s;
+    w->version += 1;
     return HG_OK;
 }
 
@@ -411,9 +667,12 @@ int hg_set_step_options(hg_world* w, const hg_step_options* o) {
     if (o->rain_mode < HG_RAIN_OFF || o->rain_mode > HG_RAIN_BERNOULLI) return fail(HG_ERR_INVALID, "bad rain_mode");
     if (!(o->rain_probability >= 0.0f && o->rain_probability <= 1.0f))
         return fail(HG_ERR_INVALID, "rain_probability must be in [0, 1]");
-    if (o->temporal_depth != HG_AUTO && (o->temporal_depth < 1 || o->temporal_depth > fused_max_depth()))
-        return fail(HG_ERR_UNSUPPORTED, "temporal_depth out of the supported range");
+    if (o->tile_x != HG_AUTO && o->tile_x != 64) return fail(HG_ERR_UNSUPPORTED, "fused tile width must be 64");
+    if (o->tile_y != HG_AUTO && o->tile_y != 16 && o->tile_y != 8)
+        return fail(HG_ERR_UNSUPPORTED, "fused tile height must be 16 or 8");
+    if (o->graph != HG_AUTO && o->graph != 0 && o->graph != 1) return fail(HG_ERR_INVALID, "graph must be -1, 0 or 1");
     w->opt = *o;
+    w->version += 1;
     return HG_OK;
 }
 
@@ -436,6 +695,7 @@ int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
     launch_scale(w->cur[S_ROCK], cells(w), w->red_f + 2 * reduction_parts(), s->out_min, s->out_max, w->stream);
     HG_CUDA(cudaGetLastError());
     w->step = 0;
+    w->dev_step_valid = false;
     return HG_OK;
 }
 
@@ -450,12 +710,14 @@ int hg_init_ks_field(hg_world* w, const hg_noise_settings* s, float base, float 
     launch_ks_from_fbm(w->ks, cells(w), base, k / amp, w->stream);
     HG_CUDA(cudaGetLastError());
     w->ks_on = true;
+    w->version += 1;
     return HG_OK;
 }
 
 int hg_clear_ks_field(hg_world* w) {
     HG_CHECK_WORLD(w);
     w->ks_on = false;
+    w->version += 1;
     return HG_OK;
 }
 
@@ -467,7 +729,10 @@ int hg_world_upload(hg_world* w, int field, const float* host) {
     DeviceGuard g(w->device);
     HG_CUDA(cudaMemcpyAsync(d, host, cells(w) * sizeof(float), cudaMemcpyHostToDevice, w->stream));
     HG_CUDA(cudaStreamSynchronize(w->stream));
-    if (field == HG_FIELD_KS) w->ks_on = true;
+    if (field == HG_FIELD_KS) {
+        w->ks_on = true;
+        w->version += 1;
+    }
     return HG_OK;
 }
 
@@ -489,7 +754,10 @@ int hg_world_upload_device(hg_world* w, int field, const float* dev) {
     if (!d) return fail(HG_ERR_INVALID, "bad field id");
     DeviceGuard g(w->device);
     HG_CUDA(cudaMemcpyAsync(d, dev, cells(w) * sizeof(float), cudaMemcpyDeviceToDevice, w->stream));
-    if (field == HG_FIELD_KS) w->ks_on = true;
+    if (field == HG_FIELD_KS) {
+        w->ks_on = true;
+        w->version += 1;
+    }
     return HG_OK;
 }
 
@@ -513,6 +781,7 @@ int hg_world_get_step(const hg_world* w, uint64_t* step) {
 int hg_world_set_step(hg_world* w, uint64_t step) {
     HG_CHECK_WORLD(w);
     w->step = step;
+    w->dev_step_valid = false;
     return HG_OK;
 }
 
@@ -543,27 +812,124 @@ int hg_step(hg_world* w, int nsteps, int mode) {
             }
             w->step += 1;
         }
-    } else {
-        int tx = 0, ty = 0;
-        if (!pick_tile(w, tx, ty))
-            return fail(HG_ERR_UNSUPPORTED, "fused mode needs n divisible by its 64x16 tile");
-        for (int k = 0; k < nsteps; ++k) {
-            FusedArgs a{};
-            a.c = c;
-            a.rain[0] = make_rain(w, w->step + 1);
-            for (int f = 0; f < S_COUNT; ++f) { a.in.f[f] = w->cur[f]; a.out.f[f] = w->alt[f]; }
-            a.u = w->u;
-            a.v = w->v;
-            a.s_ero = w->s_ero;
-            a.b_ero = w->b_ero;
-            a.err = w->err;
-            if (!launch_fused(a, w->tma, st))
-                return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a world buffer");
-            for (int f = 0; f < S_COUNT; ++f) swap(f);
-            w->step += 1;
-        }
+        if (nsteps > 0) w->dev_step_valid = false;
+    } else if (nsteps > 0) {
+        std::vector<hg_world*> one{w};
+        int rc = fused_run(w->plans, one, w->tuning, w->opt.tile_y, w->opt.graph, st, w->err, nsteps);
+        if (rc != HG_OK) return rc;
     }
     HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+
+int hg_world_tuning(const hg_world* w, int* tile_y, int* graph, double ms[4]) {
+    HG_CHECK_WORLD(w);
+    if (tile_y) *tile_y = w->tuning.th;
+    if (graph) *graph = w->tuning.graph;
+    if (ms)
+        for (int k = 0; k < 4; ++k) ms[k] = w->tuning.ms[k];
+    return HG_OK;
+}
+
+// ---- batches ---------------------------------------------------------------------
+
+int hg_batch_create(hg_world* const* worlds, int count, hg_batch** out) {
+    if (!out) return fail(HG_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if (!worlds || count < 1) return fail(HG_ERR_INVALID, "a batch needs at least one world");
+    for (int i = 0; i < count; ++i) {
+        if (!worlds[i]) return fail(HG_ERR_INVALID, "null world in batch");
+        if (worlds[i]->device != worlds[0]->device) return fail(HG_ERR_INVALID, "batch worlds must share a device");
+        for (int j = 0; j < i; ++j)
+            if (worlds[j] == worlds[i]) return fail(HG_ERR_INVALID, "a world appears twice in the batch");
+    }
+    DeviceGuard g(worlds[0]->device);
+    hg_batch* b = new (std::nothrow) hg_batch();
+    if (!b) return fail(HG_ERR_OOM, "host allocation failed");
+    b->worlds.assign(worlds, worlds + count);
+    b->device = worlds[0]->device;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        if (b->stream) cudaStreamDestroy(b->stream);
+        if (b->ev) cudaEventDestroy(b->ev);
+        cudaFree(b->err);
+        delete b;
+        return cuda_fail(e, "batch creation");
+    }
+    *out = b;
+    return HG_OK;
+}
+
+int hg_batch_destroy(hg_batch* b) {
+    if (!b) return HG_OK;
+    DeviceGuard g(b->device);
+    cudaStreamSynchronize(b->stream);
+    for (Plan*& p : b->plans) destroy_plan(p);
+    cudaEventDestroy(b->ev);
+    cudaStreamDestroy(b->stream);
+    cudaFree(b->err);
+    delete b;
+    return HG_OK;
+}
+
+int hg_batch_step(hg_batch* b, int nsteps, int mode) {
+    if (!b) return fail(HG_ERR_INVALID, "null batch");
+    if (nsteps < 0) return fail(HG_ERR_INVALID, "nsteps must be >= 0");
+    if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_FUSED_PER_WORLD)
+        return fail(HG_ERR_INVALID, "bad mode");
+    if (nsteps == 0) return HG_OK;
+    DeviceGuard g(b->device);
+    if (mode != HG_MODE_FUSED) {  // every world on its own stream, its own launches
+        for (hg_world* w : b->worlds) {
+            int rc = hg_step(w, nsteps, mode == HG_MODE_PLAIN ? HG_MODE_PLAIN : HG_MODE_FUSED);
+            if (rc != HG_OK) return rc;
+        }
+        return HG_OK;
+    }
+    // one table launch per kernel for every world: order after the worlds' streams
+    for (hg_world* w : b->worlds) {
+        HG_CUDA(cudaEventRecord(b->ev, w->stream));
+        HG_CUDA(cudaStreamWaitEvent(b->stream, b->ev, 0));
+    }
+    const hg_step_options& o = b->worlds[0]->opt;
+    int rc = fused_run(b->plans, b->worlds, b->tuning, o.tile_y, o.graph, b->stream, b->err, nsteps);
+    HG_CUDA(cudaEventRecord(b->ev, b->stream));
+    for (hg_world* w : b->worlds) HG_CUDA(cudaStreamWaitEvent(w->stream, b->ev, 0));
+    return rc;
+}
+
+int hg_batch_sync(hg_batch* b) {
+    if (!b) return fail(HG_ERR_INVALID, "null batch");
+    DeviceGuard g(b->device);
+    HG_CUDA(cudaStreamSynchronize(b->stream));
+    int flag = 0;
+    HG_CUDA(cudaMemcpy(&flag, b->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        HG_CUDA(cudaMemset(b->err, 0, sizeof(int)));
+        return fail(HG_ERR_TIMEOUT, "a fused-step tile load did not arrive within its bounded wait");
+    }
+    for (hg_world* w : b->worlds) {
+        int rc = hg_sync(w);
+        if (rc != HG_OK) return rc;
+    }
+    return HG_OK;
+}
+
+int hg_batch_stream(const hg_batch* b, void** stream) {
+    if (!b || !stream) return fail(HG_ERR_INVALID, "null argument");
+    *stream = (void*)b->stream;
+    return HG_OK;
+}
+
+int hg_batch_tuning(const hg_batch* b, int* tile_y, int* graph, double ms[4]) {
+    if (!b) return fail(HG_ERR_INVALID, "null batch");
+    if (tile_y) *tile_y = b->tuning.th;
+    if (graph) *graph = b->tuning.graph;
+    if (ms)
+        for (int k = 0; k < 4; ++k) ms[k] = b->tuning.ms[k];
     return HG_OK;
 }
 
@@ -578,6 +944,95 @@ int hg_sync(hg_world* w) {
         return fail(HG_ERR_TIMEOUT, "a fused-step tile load did not arrive within its bounded wait; "
                                     "the step's fields are not valid");
     }
+    return HG_OK;
+}
+
+namespace {
+struct CkptHeader {
+    char magic[8];  // "HGWORLD1"
+    uint32_t version;
+    int32_t n;
+    int32_t layers;
+    uint32_t nfields;
+    uint64_t step;
+    hg_erosion_settings es;
+    hg_rain_settings rs;
+    uint32_t ks_on;
+    hg_step_options opt;
+};
+const char kCkptMagic[8] = {'H', 'G', 'W', 'O', 'R', 'L', 'D', '1'};
+const int kCkptFields[] = {HG_FIELD_ROCK,   HG_FIELD_WATER,  HG_FIELD_SEDIMENT, HG_FIELD_FLUX_L, HG_FIELD_FLUX_R,
+                           HG_FIELD_FLUX_T, HG_FIELD_FLUX_B, HG_FIELD_VEL_U,    HG_FIELD_VEL_V};
+}  // namespace
+
+int hg_world_save(hg_world* w, const char* path) {
+    HG_CHECK_WORLD(w);
+    if (!path) return fail(HG_ERR_INVALID, "null path");
+    DeviceGuard g(w->device);
+    CkptHeader h{};
+    std::memcpy(h.magic, kCkptMagic, 8);
+    h.version = 1;
+    h.n = w->n;
+    h.layers = w->layers;
+    h.nfields = 9 + (w->ks_on ? 1 : 0);
+    h.step = w->step;
+    h.es = w->es;
+    h.rs = w->rs;
+    h.ks_on = w->ks_on ? 1 : 0;
+    h.opt = w->opt;
+    std::vector<float> buf(cells(w));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(HG_ERR_IO, std::string("cannot open for writing: ") + path);
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    for (uint32_t k = 0; ok && k < h.nfields; ++k) {
+        int field = k < 9 ? kCkptFields[k] : HG_FIELD_KS;
+        cudaError_t e = cudaMemcpy(buf.data(), field_ptr(w, field), buf.size() * sizeof(float), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            std::fclose(f);
+            return cuda_fail(e, "checkpoint download");
+        }
+        ok = std::fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(HG_ERR_IO, std::string("write failed: ") + path);
+    return HG_OK;
+}
+
+int hg_world_load(hg_world* w, const char* path) {
+    HG_CHECK_WORLD(w);
+    if (!path) return fail(HG_ERR_INVALID, "null path");
+    DeviceGuard g(w->device);
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(HG_ERR_IO, std::string("cannot open: ") + path);
+    CkptHeader h{};
+    if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1) {
+        std::fclose(f);
+        return fail(HG_ERR_IO, std::string("not a world checkpoint: ") + path);
+    }
+    if (h.n != w->n || h.layers != w->layers || h.nfields < 9 || h.nfields > 10) {
+        std::fclose(f);
+        return fail(HG_ERR_INVALID, "checkpoint world size or layer count differs from this world");
+    }
+    std::vector<float> buf(cells(w));
+    for (uint32_t k = 0; k < h.nfields; ++k) {
+        int field = k < 9 ? kCkptFields[k] : HG_FIELD_KS;
+        if (std::fread(buf.data(), sizeof(float), buf.size(), f) != buf.size()) {
+            std::fclose(f);
+            return fail(HG_ERR_IO, std::string("truncated checkpoint: ") + path);
+        }
+        HG_CUDA(cudaMemcpyAsync(field_ptr(w, field), buf.data(), buf.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                w->stream));
+        HG_CUDA(cudaStreamSynchronize(w->stream));
+    }
+    std::fclose(f);
+    w->step = h.step;
+    w->es = h.es;
+    w->rs = h.rs;
+    w->opt = h.opt;
+    w->ks_on = h.ks_on != 0;
+    w->dev_step_valid = false;
+    w->version += 1;
     return HG_OK;
 }
 

@@ -26,7 +26,7 @@ STATUS = {-1: "HG_ERR_INVALID", -2: "HG_ERR_OOM", -3: "HG_ERR_CUDA", -4: "HG_ERR
           -5: "HG_ERR_UNSUPPORTED", -6: "HG_ERR_IO", -7: "HG_ERR_STATE"}
 HG_AUTO = -1
 RAIN_OFF, RAIN_UNIFORM, RAIN_BERNOULLI = 0, 1, 2
-MODE_PLAIN, MODE_FUSED = 0, 1
+MODE_PLAIN, MODE_FUSED, MODE_FUSED_PER_WORLD = 0, 1, 2
 FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_t": 5, "flux_b": 6,
           "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10}
 STATE_FIELDS = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"]
@@ -58,7 +58,7 @@ class RainSettings(ctypes.Structure):
 class StepOptions(ctypes.Structure):
     _fields_ = [("rain_mode", ctypes.c_int32), ("rain_probability", ctypes.c_float),
                 ("rain_seed", ctypes.c_uint64), ("terrain_id", ctypes.c_uint32), ("thermal", ctypes.c_int32),
-                ("temporal_depth", ctypes.c_int32), ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32),
+                ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("graph", ctypes.c_int32),
                 ("reserved", ctypes.c_int32 * 6)]
 
 
@@ -101,6 +101,17 @@ def _load():
         "hg_sync": (ctypes.c_int, [P]),
         "hg_world_totals": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double)]),
         "hg_field_totals_noalloc": (ctypes.c_int, [ctypes.POINTER(P), ctypes.c_int, ctypes.c_size_t, P, P]),
+        "hg_world_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_double)]),
+        "hg_batch_create": (ctypes.c_int, [ctypes.POINTER(P), ctypes.c_int, ctypes.POINTER(P)]),
+        "hg_batch_destroy": (ctypes.c_int, [P]),
+        "hg_batch_step": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "hg_batch_sync": (ctypes.c_int, [P]),
+        "hg_batch_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
+        "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_double)]),
+        "hg_world_save": (ctypes.c_int, [P, ctypes.c_char_p]),
+        "hg_world_load": (ctypes.c_int, [P, ctypes.c_char_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -162,8 +173,8 @@ def rain_uniform(amount=0.01, period=1):
     return r
 
 
-def options(rain_mode=RAIN_UNIFORM, p=0.0, seed=0, terrain_id=0, thermal=HG_AUTO, depth=HG_AUTO,
-            tile=(HG_AUTO, HG_AUTO)):
+def options(rain_mode=RAIN_UNIFORM, p=0.0, seed=0, terrain_id=0, thermal=HG_AUTO, tile=(HG_AUTO, HG_AUTO),
+            graph=HG_AUTO):
     o = StepOptions()
     check(lib.hg_default_step_options(ctypes.byref(o)))
     o.rain_mode = rain_mode
@@ -171,8 +182,8 @@ def options(rain_mode=RAIN_UNIFORM, p=0.0, seed=0, terrain_id=0, thermal=HG_AUTO
     o.rain_seed = seed
     o.terrain_id = terrain_id
     o.thermal = thermal
-    o.temporal_depth = depth
     o.tile_x, o.tile_y = tile
+    o.graph = graph
     return o
 
 
@@ -274,11 +285,91 @@ class World:
         check(lib.hg_world_totals(self.h, out))
         return list(out)
 
+    def tuning(self):
+        th, g, ms = ctypes.c_int(), ctypes.c_int(), (ctypes.c_double * 4)()
+        check(lib.hg_world_tuning(self.h, ctypes.byref(th), ctypes.byref(g), ms))
+        return th.value, g.value, list(ms)
+
+    def save(self, path):
+        check(lib.hg_world_save(self.h, str(path).encode()))
+
+    def load(self, path):
+        check(lib.hg_world_load(self.h, str(path).encode()))
+
     @property
     def stream(self):
         p = ctypes.c_void_p()
         check(lib.hg_world_stream(self.h, ctypes.byref(p)))
         return p.value or 0
+
+
+class Batch:
+    """Several worlds stepped together (one fused launch pair per step for all)."""
+
+    def __init__(self, worlds):
+        self.worlds = list(worlds)
+        arr = (ctypes.c_void_p * len(self.worlds))(*[w.h for w in self.worlds])
+        h = ctypes.c_void_p()
+        check(lib.hg_batch_create(arr, len(self.worlds), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib.hg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, nsteps=1, mode=MODE_FUSED):
+        check(lib.hg_batch_step(self.h, nsteps, mode))
+
+    def sync(self):
+        check(lib.hg_batch_sync(self.h))
+
+    @property
+    def stream(self):
+        p = ctypes.c_void_p()
+        check(lib.hg_batch_stream(self.h, ctypes.byref(p)))
+        return p.value or 0
+
+    def tuning(self):
+        th, g, ms = ctypes.c_int(), ctypes.c_int(), (ctypes.c_double * 4)()
+        check(lib.hg_batch_tuning(self.h, ctypes.byref(th), ctypes.byref(g), ms))
+        return th.value, g.value, list(ms)
+
+
+def config3_terrains(count=64, seed=0):
+    """Ragged multi-terrain workload: side drawn from {256, 512, 1024, 2048},
+    own fBm seed, Kc log-uniform [0.05, 0.5], Ks and Kd log-uniform
+    [0.01, 0.1], Ke uniform [0.005, 0.03], talus tan uniform [0.4, 0.9],
+    config-2 rain and slippage.  Returns a list of dicts (the manifest)."""
+    import random
+    rng = random.Random(seed)
+    lu = lambda a, b: math.exp(rng.uniform(math.log(a), math.log(b)))
+    out = []
+    for i in range(count):
+        out.append(dict(n=rng.choice([256, 512, 1024, 2048]), seed=1000 + i, Kc=lu(0.05, 0.5), Ks=lu(0.01, 0.1),
+                        Kd=lu(0.01, 0.1), Ke=rng.uniform(0.005, 0.03), talus_tan=rng.uniform(0.4, 0.9)))
+    return out
+
+
+def make_config3_world(t, terrain_id=0):
+    w = World(t["n"])
+    w.init_heightmap(noise(seed=t["seed"]))
+    s = settings_config2()
+    s.Kc = t["Kc"]
+    s.Ks[0] = s.Ks[1] = t["Ks"]
+    s.Kd[0] = s.Kd[1] = t["Kd"]
+    s.Ke = t["Ke"]
+    s.Kalpha[0] = s.Kalpha[1] = math.atan(t["talus_tan"])
+    w.set_erosion(s)
+    w.set_rain(rain_uniform(0.5, 1))
+    w.set_options(options(RAIN_BERNOULLI, p=0.001, seed=t["seed"], terrain_id=terrain_id))
+    return w
 
 
 def configure(world, cfg, seed=0):

@@ -92,9 +92,10 @@ typedef struct hg_step_options {
     uint64_t rain_seed;       /* Philox key */
     uint32_t terrain_id;      /* fourth Philox counter word */
     int32_t thermal;          /* HG_AUTO: thermal passes run when Kspeed[0] != 0 */
-    int32_t temporal_depth;   /* fused mode: steps per launch, HG_AUTO = tuned */
-    int32_t tile_x;           /* fused mode tile width (HG_AUTO = tuned) */
-    int32_t tile_y;           /* fused mode tile height (HG_AUTO = tuned) */
+    int32_t tile_x;           /* fused mode tile width: HG_AUTO or 64 */
+    int32_t tile_y;           /* fused mode tile height: HG_AUTO (autotuned), 16 or 8 */
+    int32_t graph;            /* fused mode: replay a captured 2-step CUDA graph;
+                                 HG_AUTO (autotuned), 0 or 1 */
     int32_t reserved[6];
 } hg_step_options;
 
@@ -125,8 +126,9 @@ typedef struct hg_noise_settings {
 #define HG_FIELD_KS 10       /* per-cell rock solubility (replaces Ks[0]) */
 #define HG_FIELD_COUNT 11
 
-#define HG_MODE_PLAIN 0 /* one kernel per GLSL pass */
-#define HG_MODE_FUSED 1 /* one fused, tiled kernel per step (or per T steps) */
+#define HG_MODE_PLAIN 0           /* one kernel per GLSL pass */
+#define HG_MODE_FUSED 1           /* two fused, tiled kernels per step */
+#define HG_MODE_FUSED_PER_WORLD 2 /* batches only: each world's own fused launches */
 
 typedef struct hg_world hg_world;
 
@@ -197,12 +199,50 @@ int hg_world_set_step(hg_world* w, uint64_t step);
  * thermal_erosion/thermal_transport.  mode selects the per-pass kernels or
  * the fused kernel; both give bit-identical fields.  Asynchronous. */
 int hg_step(hg_world* w, int nsteps, int mode);
-/* Waits for the world's stream (the reference's glMemoryBarrier/glFinish). */
+/* Waits for the world's stream (the reference's glMemoryBarrier/glFinish).
+ * HG_ERR_TIMEOUT if a fused-step tile load gave up its bounded wait since the
+ * last sync (the step's fields are then not valid). */
 int hg_sync(hg_world* w);
+/* Fused-step variant the autotuner chose for this world (tile height 16 or 8,
+ * 0 before tuning; graph replay 0/1) and the candidates' ms per step in the
+ * order (16, direct), (16, graph), (8, direct), (8, graph).  Tuning happens
+ * in the first fused hg_step call of at least 8 steps with tile_y and graph
+ * left at HG_AUTO; its steps are ordinary steps (all variants give the same
+ * fields). */
+int hg_world_tuning(const hg_world* w, int* tile_y, int* graph, double ms[4]);
+
+/* ---- batches of worlds ---------------------------------------------------------------- */
+/* No counterpart in the reference (one map per process, src/main.cpp:222).
+ * A batch steps several worlds of any sizes (multiples of 64 for the fused
+ * mode) and settings together: in HG_MODE_FUSED one launch of each fused
+ * kernel covers every tile of every world (a table of per-world descriptors),
+ * optionally replayed from a captured CUDA graph; HG_MODE_FUSED_PER_WORLD and
+ * HG_MODE_PLAIN run each world's own launches (the one-launch-per-terrain
+ * baseline).  The batch has its own stream, ordered after and before the
+ * worlds' streams; the worlds stay usable on their own between batch steps. */
+typedef struct hg_batch hg_batch;
+int hg_batch_create(hg_world* const* worlds, int count, hg_batch** out);
+int hg_batch_destroy(hg_batch* b);
+int hg_batch_step(hg_batch* b, int nsteps, int mode);
+int hg_batch_sync(hg_batch* b);
+int hg_batch_stream(const hg_batch* b, void** stream);
+int hg_batch_tuning(const hg_batch* b, int* tile_y, int* graph, double ms[4]);
 
 /* FP64 totals over the grid, computed on the device:
  * out[0] rock, out[1] water, out[2] sediment.  Synchronises. */
 int hg_world_totals(hg_world* w, double out[3]);
+
+/* ---- checkpoint / resume ------------------------------------------------------------ */
+/* No counterpart in the reference (its state lives only in GL textures).
+ * Writes the carried fields (rock, water, sediment, four fluxes, u, v, and
+ * the per-cell solubility when set), the step counter, the erosion and rain
+ * settings and the step options to `path` (a fixed binary header, then
+ * little-endian FP32 fields).  Resuming with hg_world_load and stepping reproduces an
+ * uninterrupted run bit for bit (rain is keyed by the step counter).
+ * Synchronises.  HG_ERR_IO on file errors, HG_ERR_INVALID if the file's
+ * world size or layer count differs from w's. */
+int hg_world_save(hg_world* w, const char* path);
+int hg_world_load(hg_world* w, const char* path);
 
 /* ---- allocation-free totals -------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc

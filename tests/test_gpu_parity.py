@@ -82,17 +82,17 @@ def test_fused_bitwise_vs_float_oracle_thermal():
     assert_bitwise(w, ow)
 
 
-def test_fused_tile_option():
+@pytest.mark.parametrize("tile_y", [16, 8])
+def test_fused_tile_option(tile_y):
     a, _, _, _ = make_pair(256, "config2", p=0.01)
     b, _, _, _ = make_pair(256, "config2", p=0.01)
-    b.set_options(H.options(H.RAIN_BERNOULLI, p=0.01, tile=(64, 16)))
+    b.set_options(H.options(H.RAIN_BERNOULLI, p=0.01, tile=(64, tile_y)))
     a.step(40, H.MODE_PLAIN)
     b.step(40, H.MODE_FUSED)
     for f in STATE:
         assert np.array_equal(a.download(f), b.download(f)), f
-    b.set_options(H.options(H.RAIN_BERNOULLI, p=0.01, tile=(32, 32)))
     with pytest.raises(H.HydrogenError) as e:
-        b.step(1, H.MODE_FUSED)
+        b.set_options(H.options(H.RAIN_BERNOULLI, p=0.01, tile=(32, 32)))
     assert e.value.code == -5
 
 
