@@ -97,6 +97,34 @@ void launch_fused_table(const TerrainDesc* tds, const int* tile0, int nterr, int
 // Same for one terrain whose descriptor travels as a kernel parameter.
 void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st);
 
+// ---- adjoint (hg_adjoint.cu) ----------------------------------------------------------
+// A step's state or its adjoint: rock, water, sediment, fL, fR, fT, fB.
+struct AdjFields {
+    float* b;
+    float* d;
+    float* s;
+    float* f[4];
+};
+// Forward intermediates recomputed for the reversed step.
+struct AdjTemps {
+    float *dr, *u, *v, *vz, *d2, *be, *se;
+};
+// Adjoint work fields: per-cell terms and neighbour packets.
+struct AdjWork {
+    float *dse, *du, *dv, *dvz, *dd2, *rb, *rs, *pdx, *pdz, *wbar, *gd1;
+    float* pdh[4];
+    float* pin[4];
+    float* fown[4];
+};
+constexpr int ADJ_WORK_FIELDS = 23;
+// Reverses one step: A (adjoint of the step's outputs) -> R (adjoint of its
+// inputs X); accumulates the per-cell Ks gradient into dks.
+void launch_adjoint_step(const StepConsts& c, const RainStep& r, const AdjFields& X, const AdjFields& A,
+                         const AdjFields& R, const AdjTemps& T, const AdjWork& W, float* dks, cudaStream_t st);
+// loss = mean((b - target)^2) into *out (device), grad = dloss/db (optional).
+void launch_mse(const float* b, const float* target, size_t count, float* grad, double* part, int nparts,
+                double* out, cudaStream_t st);
+
 // ---- init and reductions (hg_init.cu) ---------------------------------------------
 void launch_fbm_raw(float* out, int n, const hg_noise_settings& s, cudaStream_t st);
 // min and max of a device array into two floats of `minmax` (device).

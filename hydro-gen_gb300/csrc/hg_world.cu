@@ -947,6 +947,221 @@ int hg_sync(hg_world* w) {
     return HG_OK;
 }
 
+// ---- differentiation ---------------------------------------------------------------
+
+struct hg_tape {
+    hg_world* w = nullptr;
+    hg_world* shadow = nullptr;  // recomputes segments from checkpoints
+    int nsteps = 0, K = 0, nseg = 0;
+    uint64_t step0 = 0;
+    bool recorded = false;
+    float* ckpt = nullptr;  // nseg states (segment starts)
+    float* seg = nullptr;   // K states (inputs of a segment's steps)
+    float* adj = nullptr;   // 2 adjoint states
+    float* temps = nullptr; // 7 recomputed fields
+    float* work = nullptr;  // ADJ_WORK_FIELDS fields
+    float* dks = nullptr;   // per-cell Ks gradient
+};
+
+namespace {
+constexpr int kStateFields = 7;
+
+AdjFields fields_at(float* base, size_t c) {
+    AdjFields f;
+    f.b = base;
+    f.d = base + c;
+    f.s = base + 2 * c;
+    for (int k = 0; k < 4; ++k) f.f[k] = base + (3 + k) * c;
+    return f;
+}
+
+void free_tape(hg_tape* t) {
+    cudaFree(t->ckpt); cudaFree(t->seg); cudaFree(t->adj); cudaFree(t->temps); cudaFree(t->work);
+    cudaFree(t->dks);
+    if (t->shadow) hg_world_destroy(t->shadow);
+}
+
+// state fields of a world (current buffers) -> contiguous state at dst
+int copy_state_out(hg_world* w, float* dst, cudaStream_t st) {
+    size_t c = cells(w);
+    for (int f = 0; f < kStateFields; ++f)
+        HG_CUDA(cudaMemcpyAsync(dst + f * c, w->cur[f], c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    return HG_OK;
+}
+
+int copy_state_in(hg_world* w, const float* src, cudaStream_t st) {
+    size_t c = cells(w);
+    for (int f = 0; f < kStateFields; ++f)
+        HG_CUDA(cudaMemcpyAsync(w->cur[f], src + f * c, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    return HG_OK;
+}
+}  // namespace
+
+int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
+    HG_CHECK_WORLD(w);
+    if (!out) return fail(HG_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if (nsteps < 1) return fail(HG_ERR_INVALID, "nsteps must be >= 1");
+    if (thermal_on(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion");
+    if (!fused_tile_ok(w->n, 16)) return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
+    DeviceGuard g(w->device);
+    const size_t c = cells(w), state_bytes = kStateFields * c * sizeof(float);
+    int K = ckpt_every;
+    if (K == HG_AUTO || K <= 0) {
+        // memory holds nsteps/K checkpoints plus K segment states: ~sqrt(nsteps)
+        K = (int)std::ceil(std::sqrt((double)nsteps));
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+            size_t fit = free_b / 2 / state_bytes;  // keep half of the free memory
+            while (K > 1 && (size_t)(K + (nsteps + K - 1) / K) > fit) --K;
+        }
+    }
+    K = std::min(K, nsteps);
+    hg_tape* t = new (std::nothrow) hg_tape();
+    if (!t) return fail(HG_ERR_OOM, "host allocation failed");
+    t->w = w;
+    t->nsteps = nsteps;
+    t->K = K;
+    t->nseg = (nsteps + K - 1) / K;
+    cudaError_t e = cudaMalloc((void**)&t->ckpt, t->nseg * state_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->seg, (size_t)K * state_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->adj, 2 * state_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->temps, state_bytes);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->work, ADJ_WORK_FIELDS * c * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->dks, c * sizeof(float));
+    if (e != cudaSuccess) {
+        free_tape(t);
+        delete t;
+        int code = e == cudaErrorMemoryAllocation ? HG_ERR_OOM : HG_ERR_CUDA;
+        cudaGetLastError();
+        return fail(code, std::string("tape allocation: ") + cudaGetErrorString(e));
+    }
+    int rc = hg_world_create(w->n, w->layers, &t->shadow);
+    if (rc != HG_OK) {
+        free_tape(t);
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return HG_OK;
+}
+
+int hg_tape_destroy(hg_tape* t) {
+    if (!t) return HG_OK;
+    DeviceGuard g(t->w->device);
+    cudaStreamSynchronize(t->w->stream);
+    free_tape(t);
+    delete t;
+    return HG_OK;
+}
+
+int hg_tape_info(const hg_tape* t, int* nsteps, int* ckpt_every) {
+    if (!t) return fail(HG_ERR_INVALID, "null tape");
+    if (nsteps) *nsteps = t->nsteps;
+    if (ckpt_every) *ckpt_every = t->K;
+    return HG_OK;
+}
+
+int hg_forward(hg_tape* t) {
+    if (!t) return fail(HG_ERR_INVALID, "null tape");
+    hg_world* w = t->w;
+    if (thermal_on(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion");
+    DeviceGuard g(w->device);
+    t->step0 = w->step;
+    const size_t c = cells(w);
+    for (int s = 0; s < t->nseg; ++s) {
+        int rc = copy_state_out(w, t->ckpt + (size_t)s * kStateFields * c, w->stream);
+        if (rc != HG_OK) return rc;
+        rc = hg_step(w, std::min(t->K, t->nsteps - s * t->K), HG_MODE_FUSED);
+        if (rc != HG_OK) return rc;
+    }
+    t->recorded = true;
+    return HG_OK;
+}
+
+int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* dL_drock0) {
+    if (!t) return fail(HG_ERR_INVALID, "null tape");
+    if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
+    if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
+    hg_world* w = t->w;
+    hg_world* sh = t->shadow;
+    DeviceGuard g(w->device);
+    cudaStream_t st = w->stream;
+    const size_t c = cells(w), sf = kStateFields * c;
+    // the shadow world recomputes segments with the world's settings
+    sh->es = w->es;
+    sh->rs = w->rs;
+    sh->opt = w->opt;
+    sh->version += 1;
+    if (w->ks_on) HG_CUDA(cudaMemcpyAsync(sh->ks, w->ks, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    sh->ks_on = w->ks_on;
+    const StepConsts cst = make_consts(w);
+    AdjFields A = fields_at(t->adj, c), R = fields_at(t->adj + sf, c);
+    AdjTemps T;
+    float* tp = t->temps;
+    T.dr = tp; T.u = tp + c; T.v = tp + 2 * c; T.vz = tp + 3 * c; T.d2 = tp + 4 * c; T.be = tp + 5 * c;
+    T.se = tp + 6 * c;
+    AdjWork W;
+    float* wp = t->work;
+    float** named[] = {&W.dse, &W.du, &W.dv, &W.dvz, &W.dd2, &W.rb, &W.rs, &W.pdx, &W.pdz, &W.wbar, &W.gd1};
+    int k = 0;
+    for (float** p : named) *p = wp + (size_t)(k++) * c;
+    for (int d = 0; d < 4; ++d) {
+        W.pdh[d] = wp + (size_t)(k++) * c;
+        W.pin[d] = wp + (size_t)(k++) * c;
+        W.fown[d] = wp + (size_t)(k++) * c;
+    }
+    HG_CUDA(cudaMemsetAsync(t->adj, 0, 2 * sf * sizeof(float), st));
+    HG_CUDA(cudaMemcpyAsync(A.b, dL_drock_final, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    HG_CUDA(cudaMemsetAsync(t->dks, 0, c * sizeof(float), st));
+    cudaEvent_t ev;
+    HG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    int rc = HG_OK;
+    for (int s = t->nseg - 1; s >= 0 && rc == HG_OK; --s) {
+        const int len = std::min(t->K, t->nsteps - s * t->K);
+        const float* ck = t->ckpt + (size_t)s * sf;
+        HG_CUDA(cudaMemcpyAsync(t->seg, ck, sf * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        if (len > 1) {  // inputs of the segment's later steps, recomputed on the shadow world
+            if ((rc = copy_state_in(sh, ck, st)) != HG_OK) break;
+            HG_CUDA(cudaEventRecord(ev, st));
+            HG_CUDA(cudaStreamWaitEvent(sh->stream, ev, 0));
+            sh->step = t->step0 + (uint64_t)s * t->K;
+            sh->dev_step_valid = false;
+            for (int j = 1; j < len && rc == HG_OK; ++j) {
+                rc = hg_step(sh, 1, HG_MODE_FUSED);
+                if (rc == HG_OK) rc = copy_state_out(sh, t->seg + (size_t)j * sf, sh->stream);
+            }
+            HG_CUDA(cudaEventRecord(ev, sh->stream));
+            HG_CUDA(cudaStreamWaitEvent(st, ev, 0));
+        }
+        for (int j = len - 1; j >= 0 && rc == HG_OK; --j) {
+            AdjFields X = fields_at(t->seg + (size_t)j * sf, c);
+            RainStep r = make_rain(w, t->step0 + (uint64_t)s * t->K + j + 1);
+            launch_adjoint_step(cst, r, X, A, R, T, W, t->dks, st);
+            std::swap(A, R);
+        }
+    }
+    cudaEventDestroy(ev);
+    if (rc != HG_OK) return rc;
+    if (dL_drock0) HG_CUDA(cudaMemcpyAsync(dL_drock0, A.b, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    if (dL_dks) HG_CUDA(cudaMemcpyAsync(dL_dks, t->dks, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+
+int hg_mse(hg_world* w, const float* target, double* loss, float* dL_drock) {
+    HG_CHECK_WORLD(w);
+    if (!target || !loss) return fail(HG_ERR_INVALID, "null target or loss");
+    DeviceGuard g(w->device);
+    const int parts = reduction_parts();
+    double* res = w->red_d + 8 * parts;
+    launch_mse(w->cur[S_ROCK], target, cells(w), dL_drock, w->red_d, parts, res, w->stream);
+    HG_CUDA(cudaGetLastError());
+    HG_CUDA(cudaMemcpyAsync(loss, res, sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    return HG_OK;
+}
+
 namespace {
 struct CkptHeader {
     char magic[8];  // "HGWORLD1"

@@ -110,6 +110,12 @@ def _load():
         "hg_batch_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
         "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_double)]),
+        "hg_tape_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(P)]),
+        "hg_tape_destroy": (ctypes.c_int, [P]),
+        "hg_tape_info": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+        "hg_forward": (ctypes.c_int, [P]),
+        "hg_backward": (ctypes.c_int, [P, P, P, P]),
+        "hg_mse": (ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_double), P]),
         "hg_world_save": (ctypes.c_int, [P, ctypes.c_char_p]),
         "hg_world_load": (ctypes.c_int, [P, ctypes.c_char_p]),
     }
@@ -301,6 +307,47 @@ class World:
         p = ctypes.c_void_p()
         check(lib.hg_world_stream(self.h, ctypes.byref(p)))
         return p.value or 0
+
+
+class Tape:
+    """Checkpointed record of nsteps steps of a world for hg_backward."""
+
+    def __init__(self, world, nsteps, ckpt_every=HG_AUTO):
+        h = ctypes.c_void_p()
+        check(lib.hg_tape_create(world.h, nsteps, ckpt_every, ctypes.byref(h)))
+        self.h = h
+        self.world = world
+
+    def close(self):
+        if self.h:
+            lib.hg_tape_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ckpt_every(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        check(lib.hg_tape_info(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return b.value
+
+    def forward(self):
+        check(lib.hg_forward(self.h))
+
+    def backward(self, dl_drock_ptr, dl_dks_ptr=None, dl_drock0_ptr=None):
+        """Device pointers (e.g. torch tensors' data_ptr())."""
+        check(lib.hg_backward(self.h, ctypes.c_void_p(dl_drock_ptr), ctypes.c_void_p(dl_dks_ptr or 0),
+                              ctypes.c_void_p(dl_drock0_ptr or 0)))
+
+
+def mse(world, target_ptr, grad_ptr=None):
+    loss = ctypes.c_double()
+    check(lib.hg_mse(world.h, ctypes.c_void_p(target_ptr), ctypes.byref(loss), ctypes.c_void_p(grad_ptr or 0)))
+    return loss.value
 
 
 class Batch:

@@ -232,6 +232,34 @@ int hg_batch_tuning(const hg_batch* b, int* tile_y, int* graph, double ms[4]);
  * out[0] rock, out[1] water, out[2] sediment.  Synchronises. */
 int hg_world_totals(hg_world* w, double out[3]);
 
+/* ---- differentiation ------------------------------------------------------------------ */
+/* No counterpart in the reference.  Reverse-mode adjoint of the step without
+ * thermal erosion (the talus passes must be off: Kspeed[0] == 0 or thermal
+ * option 0), for fitting the per-cell rock solubility and the initial rock
+ * heights.  A tape records nsteps steps of w with a checkpoint of the carried
+ * fields every ckpt_every steps (HG_AUTO: about sqrt(nsteps), fewer if free
+ * device memory is short); hg_backward recomputes each segment from its
+ * checkpoint and runs the reverse kernels.  Subgradients at max/min/clamp
+ * and at the dissolve/deposit branches: the taken branch's derivative.
+ * The world's settings and per-cell Ks must not change between hg_forward
+ * and hg_backward. */
+typedef struct hg_tape hg_tape;
+int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out);
+int hg_tape_destroy(hg_tape* t);
+int hg_tape_info(const hg_tape* t, int* nsteps, int* ckpt_every);
+/* Advances w by the tape's nsteps fused steps, recording checkpoints. */
+int hg_forward(hg_tape* t);
+/* Device pointers (n*n floats): dL_drock_final is the loss gradient with
+ * respect to the rock field after the recorded steps; outputs (either may be
+ * NULL) are the gradients with respect to the per-cell Ks (Ks[0] of every cell
+ * when no field is set) and to the rock field before the steps.  Ordered on
+ * the world's stream. */
+int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* dL_drock0);
+/* loss = mean((rock - target)^2) over the grid (FP64 sum) and, if dL_drock is
+ * not NULL, its gradient 2*(rock - target)/n^2; target and dL_drock are device
+ * pointers.  Synchronises. */
+int hg_mse(hg_world* w, const float* target, double* loss, float* dL_drock);
+
 /* ---- checkpoint / resume ------------------------------------------------------------ */
 /* No counterpart in the reference (its state lives only in GL textures).
  * Writes the carried fields (rock, water, sediment, four fluxes, u, v, and

@@ -237,3 +237,43 @@ def num_threads():
 
 def set_num_threads(t):
     lib.hgo_set_num_threads(t)
+
+
+# ---- FP64 reference adjoint (hg_adjoint_ref.cpp) ------------------------------------
+lib.hgo_adjoint_ref.restype = ctypes.c_int
+lib.hgo_adjoint_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                ctypes.c_void_p, ctypes.c_void_p]
+lib.hgo_forward_ref.restype = ctypes.c_int
+lib.hgo_forward_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+
+
+def _adj_settings(s, amount):
+    return np.array([s.d_t, s.G, s.ENERGY_KEPT, s.Kc, s.Kd[0], s.Ke, amount], dtype=np.float32)
+
+
+def adjoint_ref(settings, amount, period, b0, ks, target, nsteps, step0=0):
+    """FP64 reference: loss = mean((rock_final - target)^2) after nsteps of the
+    thermal-free single-material step; returns (loss, dL/dKs, dL/drock0)."""
+    n = b0.shape[0]
+    st = _adj_settings(settings, amount)
+    b0 = np.ascontiguousarray(b0, dtype=np.float64)
+    ks = np.ascontiguousarray(ks, dtype=np.float32)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    loss = ctypes.c_double()
+    dks = np.empty((n, n)); db0 = np.empty((n, n))
+    rc = lib.hgo_adjoint_ref(n, st.ctypes.data, period, step0, nsteps, b0.ctypes.data, ks.ctypes.data, tg.ctypes.data,
+                             ctypes.byref(loss), dks.ctypes.data, db0.ctypes.data)
+    assert rc == 0
+    return loss.value, dks, db0
+
+
+def forward_ref(settings, amount, period, b0, ks, nsteps, step0=0):
+    n = b0.shape[0]
+    st = _adj_settings(settings, amount)
+    b0 = np.ascontiguousarray(b0, dtype=np.float64)
+    ks = np.ascontiguousarray(ks, dtype=np.float32)
+    out = np.empty((n, n))
+    lib.hgo_forward_ref(n, st.ctypes.data, period, step0, nsteps, b0.ctypes.data, ks.ctypes.data, out.ctypes.data)
+    return out
