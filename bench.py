@@ -26,6 +26,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "hydro-gen_gb300"))
 
@@ -43,6 +45,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_GRID)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
     return ap.parse_args()
 
 
@@ -135,6 +138,93 @@ def cpu_baseline(n_sample=1024, budget_s=12.0):
     return {"value": steps * n_sample * n_sample / el, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
             "sample": f"{n_sample}x{n_sample} world, same physics and rain, {steps} steps in {el:.1f} s "
                       f"(float oracle, OpenMP over rows)"}
+
+
+def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3):
+    """Forward + adjoint of the inverse-erosion workload: 1024^2, config-1
+    physics, per-cell Ks = 0.05 exp(0.5 n(x)) from 3-octave simplex noise,
+    MSE to a target, gradients for Ks and the initial rock."""
+    w = H.World(n)
+    w.init_heightmap(H.noise(seed=0))
+    H.configure(w, "config1")
+    w.init_ks_field(H.noise(seed=7, octaves=3, frequency=1.0 / 256), 0.05, 0.5)
+    w.step(nsteps, H.MODE_FUSED)
+    target = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    w.download_device("rock", target.data_ptr())
+    w.init_heightmap(H.noise(seed=0))
+    b0 = w.download("rock")
+    g = torch.empty_like(target)
+    dks = torch.empty_like(target)
+    db0 = torch.empty_like(target)
+    tape = H.Tape(w, nsteps, ckpt)
+    stream = torch.cuda.ExternalStream(w.stream)
+
+    def reset():
+        w.upload("rock", b0)
+        for f in ("water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b"):
+            w.upload(f, np.zeros((n, n), np.float32))
+        w.step_count = 0
+
+    fwd_ms, all_ms = [], []
+    for r in range(reps + 1):
+        reset()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        tape.forward()
+        e1.record(stream)
+        H.mse(w, target.data_ptr(), g.data_ptr())
+        tape.backward(g.data_ptr(), dks.data_ptr(), db0.data_ptr())
+        e2.record(stream)
+        e2.synchronize()
+        if r:
+            fwd_ms.append(e0.elapsed_time(e1))
+            all_ms.append(e0.elapsed_time(e2))
+    f, a = statistics.median(fwd_ms), statistics.median(all_ms)
+    cs = n * n * nsteps
+    return {"workload": f"inverse erosion {n}x{n}, {nsteps} steps, per-cell Ks, checkpoints every {ckpt}",
+            "forward_cell_steps_per_s": cs / (f / 1e3), "fwd_adjoint_cell_steps_per_s": cs / (a / 1e3),
+            "fwd_adjoint_over_forward_time": a / f, "ms_forward": f, "ms_fwd_adjoint": a}
+
+
+def bench_batch(H, torch, count=64, nsteps=50, warmup=16):
+    """64 terrains of sides drawn from {256, 512, 1024, 2048} with their own
+    seeds and parameters, stepped three ways: each terrain's own fused
+    launches, one table launch per kernel for all terrains (tile height and
+    graph replay fixed to the table's tuned choice), and the batch API's
+    autotuned form (the faster of the two)."""
+    ts = H.config3_terrains(count=count, seed=0)
+    ws = [H.make_config3_world(t, terrain_id=i) for i, t in enumerate(ts)]
+    cells = sum(t["n"] ** 2 for t in ts)
+    out = {"workload": f"{count} terrains, sides from {{256,512,1024,2048}}, {cells} cells", "steps": nsteps}
+
+    def timed(b, mode):
+        b.step(warmup, mode)
+        b.sync()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.step(nsteps, mode)
+        b.sync()
+        torch.cuda.synchronize()
+        return cells * nsteps / (time.perf_counter() - t0)
+
+    b = H.Batch(ws)
+    out["per_terrain_cell_steps_per_s"] = timed(b, H.MODE_FUSED_PER_WORLD)
+    out["autotuned_cell_steps_per_s"] = timed(b, H.MODE_FUSED)
+    th, graph, ms = b.tuning()
+    per_world, ms_pw = b.launch_form()
+    out["tuned"] = {"form": "per_terrain" if per_world else "one_launch", "tile": [64, th], "graph": graph,
+                    "one_launch_ms_per_step": ms, "per_terrain_ms_per_step": ms_pw}
+    b.close()
+    for i, (w, t) in enumerate(zip(ws, ts)):
+        w.set_options(H.options(H.RAIN_BERNOULLI, p=0.001, seed=t["seed"], terrain_id=i, tile=(64, th),
+                                graph=graph))
+    b = H.Batch(ws)
+    out["one_launch_cell_steps_per_s"] = timed(b, H.MODE_FUSED)
+    b.close()
+    out["one_launch_over_per_terrain"] = out["one_launch_cell_steps_per_s"] / out["per_terrain_cell_steps_per_s"]
+    for w in ws:
+        w.close()
+    return out
 
 
 def run_reference(args, rank):
@@ -274,6 +364,9 @@ def main():
         "e2e": {"value": world_size * cells * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
     }
+    if not args.no_extras:
+        line["fwd_adjoint"] = bench_adjoint(H, torch)
+        line["batch"] = bench_batch(H, torch)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)

@@ -75,11 +75,11 @@ __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float at4(const float4& v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
 
-__device__ __forceinline__ int find_terrain(const int* __restrict__ tile0, int nterr, int tile) {
+__device__ __forceinline__ int find_terrain(const int* tile0, int nterr, int tile) {
     int lo = 0, hi = nterr - 1;
     while (lo < hi) {  // last terrain whose first tile <= tile
         int mid = (lo + hi + 1) >> 1;
-        if (__ldg(tile0 + mid) <= tile) lo = mid; else hi = mid - 1;
+        if (tile0[mid] <= tile) lo = mid; else hi = mid - 1;
     }
     return lo;
 }
@@ -101,8 +101,8 @@ __device__ __forceinline__ RainStep rain_for(const RainBase& rb, unsigned long l
 // k_hydro
 // ---------------------------------------------------------------------------
 template <int TH, bool EDGE>
-__device__ __forceinline__ void hydro_tile(const TerrainDesc& td, float* sm, uint64_t* bar, int tx0, int ty0,
-                                           int* err) {
+__device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorMap* maps, float* sm, uint64_t* bar,
+                                           int tx0, int ty0, int* err) {
     using G = Geo<TH>;
     constexpr int NTH = G::NTH, H_RC = G::H_RC, H_RH = G::H_RH;
     const StepConsts& c = td.c;
@@ -113,7 +113,7 @@ __device__ __forceinline__ void hydro_tile(const TerrainDesc& td, float* sm, uin
     if (tid == 0) {
         mbar_arrive_expect_tx(bar, H_N * G::H_BOX * sizeof(float));
 #pragma unroll
-        for (int f = 0; f < H_N; ++f) tma_load_2d(sm + f * H_RC, &td.maps[f], gx0, gy0, bar);
+        for (int f = 0; f < H_N; ++f) tma_load_2d(sm + f * H_RC, &maps[f], gx0, gy0, bar);
     }
     // rain words of the region's row groups, drawn while the tiles load
     constexpr int RG = (RW / 4) * H_RH;
@@ -199,7 +199,7 @@ __device__ __forceinline__ void hydro_tile(const TerrainDesc& td, float* sm, uin
 }
 
 template <int TH>
-__device__ __forceinline__ void hydro_block(const TerrainDesc& td, int tile, int* err) {
+__device__ __forceinline__ void hydro_block(const TerrainHot& td, const CUtensorMap* maps, int tile, int* err) {
     using G = Geo<TH>;
     __shared__ __align__(128) float sm[H_N * G::H_RC];
     __shared__ __align__(8) uint64_t bar;
@@ -208,23 +208,24 @@ __device__ __forceinline__ void hydro_block(const TerrainDesc& td, int tile, int
     const int n = td.c.n;
     const int tx0 = (tile % td.tiles_x) * TW, ty0 = (tile / td.tiles_x) * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 1 >= 0 && ty0 + TH + 1 <= n;
-    if (inner) hydro_tile<TH, false>(td, sm, &bar, tx0, ty0, err);
-    else hydro_tile<TH, true>(td, sm, &bar, tx0, ty0, err);
+    if (inner) hydro_tile<TH, false>(td, maps, sm, &bar, tx0, ty0, err);
+    else hydro_tile<TH, true>(td, maps, sm, &bar, tx0, ty0, err);
 }
 
-// Batch form: descriptors in global memory, the block finds its terrain.
+// Batch form: the terrain records are a kernel parameter (constant bank),
+// the block finds its terrain by binary search.
 template <int TH>
-__global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro(const TerrainDesc* __restrict__ tds,
-                                                        const int* __restrict__ tile0, int nterr, int* err) {
-    const int t = find_terrain(tile0, nterr, blockIdx.x);
-    hydro_block<TH>(tds[t], blockIdx.x - __ldg(tile0 + t), err);
+__global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro(const __grid_constant__ BatchParams bp,
+                                                        const CUtensorMap* __restrict__ maps, int* err) {
+    const int t = find_terrain(bp.tile0, bp.nterr, blockIdx.x);
+    hydro_block<TH>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
 }
 
-// Single-world form: the descriptor is a kernel parameter, so the step
-// constants are read from the constant bank.
+// Single-world form: the whole descriptor, tensor maps included, is a kernel
+// parameter.
 template <int TH>
 __global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro1(const __grid_constant__ TerrainDesc td, int* err) {
-    hydro_block<TH>(td, blockIdx.x, err);
+    hydro_block<TH>(td.h, td.maps, blockIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -260,8 +261,8 @@ __device__ __forceinline__ void outflows_scalar(const StepConsts& c, const float
 }
 
 template <int TH, bool EDGE>
-__device__ __forceinline__ void transport_tile(const TerrainDesc& td, float* be, float* outf, uint64_t* bar,
-                                               int tx0, int ty0, int* err) {
+__device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUtensorMap* maps, float* be, float* outf,
+                                               uint64_t* bar, int tx0, int ty0, int* err) {
     using G = Geo<TH>;
     constexpr int NTH = G::NTH, O_C = G::O_C;
     const StepConsts& c = td.c;
@@ -270,7 +271,7 @@ __device__ __forceinline__ void transport_tile(const TerrainDesc& td, float* be,
     const int gx0 = tx0 - HX, gy0 = ty0 - 2;
     if (c.thermal && tid == 0) {
         mbar_arrive_expect_tx(bar, G::T_BOX * sizeof(float));
-        tma_load_2d(be, &td.maps[M_BERO], gx0, gy0, bar);
+        tma_load_2d(be, &maps[M_BERO], gx0, gy0, bar);
     }
     const int iy = tid / GPR, g = tid % GPR;
     const int x0 = tx0 + 4 * g, y = ty0 + iy;
@@ -382,7 +383,7 @@ __device__ __forceinline__ void transport_tile(const TerrainDesc& td, float* be,
 }
 
 template <int TH>
-__device__ __forceinline__ void transport_block(const TerrainDesc& td, int tile, int* err) {
+__device__ __forceinline__ void transport_block(const TerrainHot& td, const CUtensorMap* maps, int tile, int* err) {
     using G = Geo<TH>;
     __shared__ __align__(128) float be[G::T_BOX];
     __shared__ __align__(16) float outf[8 * G::O_C];
@@ -392,23 +393,23 @@ __device__ __forceinline__ void transport_block(const TerrainDesc& td, int tile,
     const int n = td.c.n;
     const int tx0 = (tile % td.tiles_x) * TW, ty0 = (tile / td.tiles_x) * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 2 >= 0 && ty0 + TH + 2 <= n;
-    if (inner) transport_tile<TH, false>(td, be, outf, &bar, tx0, ty0, err);
-    else transport_tile<TH, true>(td, be, outf, &bar, tx0, ty0, err);
+    if (inner) transport_tile<TH, false>(td, maps, be, outf, &bar, tx0, ty0, err);
+    else transport_tile<TH, true>(td, maps, be, outf, &bar, tx0, ty0, err);
     // k_hydro of this step has finished (stream order) and the next step's
     // k_hydro starts after this launch: advance the terrain's step counter
     if (tile == 0 && threadIdx.x == 0) *td.step += 1ull;
 }
 
 template <int TH>
-__global__ void __launch_bounds__(Geo<TH>::NTH) k_transport(const TerrainDesc* __restrict__ tds,
-                                                            const int* __restrict__ tile0, int nterr, int* err) {
-    const int t = find_terrain(tile0, nterr, blockIdx.x);
-    transport_block<TH>(tds[t], blockIdx.x - __ldg(tile0 + t), err);
+__global__ void __launch_bounds__(Geo<TH>::NTH) k_transport(const __grid_constant__ BatchParams bp,
+                                                            const CUtensorMap* __restrict__ maps, int* err) {
+    const int t = find_terrain(bp.tile0, bp.nterr, blockIdx.x);
+    transport_block<TH>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
 }
 
 template <int TH>
 __global__ void __launch_bounds__(Geo<TH>::NTH) k_transport1(const __grid_constant__ TerrainDesc td, int* err) {
-    transport_block<TH>(td, blockIdx.x, err);
+    transport_block<TH>(td.h, td.maps, blockIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -457,36 +458,37 @@ bool fused_tile_ok(int n, int th) { return (th == 16 || th == 8) && n % TW == 0 
 int fused_tiles(int n, int th) { return (n / TW) * (n / th); }
 
 bool fill_desc(TerrainDesc& d, const TerrainSrc& s, int th, int tile0, TmaCache& cache) {
-    d.c = s.c;
-    d.rain = s.rain;
-    for (int f = 0; f < S_COUNT; ++f) d.out[f] = s.out[f];
-    d.u = s.u;
-    d.v = s.v;
-    d.s_ero = s.s_ero;
-    d.b_ero = s.b_ero;
-    d.step = s.step;
-    d.tiles_x = s.c.n / TW;
-    d.tile0 = tile0;
+    TerrainHot& h = d.h;
+    h.c = s.c;
+    h.rain = s.rain;
+    for (int f = 0; f < S_COUNT; ++f) h.out[f] = s.out[f];
+    h.u = s.u;
+    h.v = s.v;
+    h.s_ero = s.s_ero;
+    h.b_ero = s.b_ero;
+    h.step = s.step;
+    h.tiles_x = s.c.n / TW;
+    h.tile0 = tile0;
     const int in_fields[H_N] = {S_ROCK, S_WATER, S_SED, S_FL, S_FR, S_FT, S_FB};
     for (int f = 0; f < H_N; ++f)
         if (!cache.get(s.in[in_fields[f]], s.c.n, th + 2, &d.maps[f])) return false;
     return cache.get(s.b_ero, s.c.n, th + 4, &d.maps[M_BERO]);
 }
 
-void launch_fused_table(const TerrainDesc* tds, const int* tile0, int nterr, int total_tiles, int th, int* err,
+void launch_fused_table(const BatchParams& bp, const CUtensorMap* maps, int total_tiles, int th, int* err,
                         cudaStream_t st) {
     if (th == 16) {
-        k_hydro<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(tds, tile0, nterr, err);
-        k_transport<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(tds, tile0, nterr, err);
+        k_hydro<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(bp, maps, err);
+        k_transport<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(bp, maps, err);
     } else {
-        k_hydro<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(tds, tile0, nterr, err);
-        k_transport<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(tds, tile0, nterr, err);
+        k_hydro<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(bp, maps, err);
+        k_transport<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(bp, maps, err);
     }
     count_launch(2);
 }
 
 void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st) {
-    const int tiles = fused_tiles(td.c.n, th);
+    const int tiles = fused_tiles(td.h.c.n, th);
     if (th == 16) {
         k_hydro1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);
         k_transport1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);

@@ -45,11 +45,8 @@ struct RainBase {
     uint32_t seed_lo, seed_hi, terrain_id;
 };
 
-// One terrain (world) of a fused launch, as the kernels read it from global
-// memory.  maps[0..6]: TMA boxes of the step's input rock, water, sediment,
-// fL, fR, fT, fB; maps[7]: eroded rock.  (CUtensorMap makes it 64-byte aligned.)
-struct TerrainDesc {
-    CUtensorMap maps[8];
+// One terrain (world) of a fused launch, without its tensor maps.
+struct TerrainHot {
     StepConsts c;
     RainBase rain;
     float* out[S_COUNT];
@@ -61,6 +58,22 @@ struct TerrainDesc {
     int tiles_x;
     int tile0;  // first tile of this terrain in the launch
 };
+// maps[0..6]: TMA boxes of the step's input rock, water, sediment, fL, fR,
+// fT, fB; maps[7]: eroded rock.  (CUtensorMap makes it 64-byte aligned.)
+constexpr int MAPS_PER_TERRAIN = 8;
+struct TerrainDesc {
+    CUtensorMap maps[MAPS_PER_TERRAIN];
+    TerrainHot h;
+};
+// A batch launch's terrain records travel as one kernel parameter (read
+// through the constant bank); the tensor maps stay in global memory.
+constexpr int MAX_BATCH = 128;
+struct BatchParams {
+    int nterr;
+    int tile0[MAX_BATCH];
+    TerrainHot t[MAX_BATCH];
+};
+static_assert(sizeof(BatchParams) < 32000, "kernel parameter space");
 
 // Host view of one terrain for one step direction (inputs -> outputs).
 struct TerrainSrc {
@@ -91,8 +104,9 @@ bool fused_tile_ok(int n, int th);
 int fused_tiles(int n, int th);
 // Fills a descriptor (tensor maps from the cache); false if a map cannot be encoded.
 bool fill_desc(TerrainDesc& d, const TerrainSrc& s, int th, int tile0, TmaCache& cache);
-// k_hydro then k_transport over every tile of the table's terrains.
-void launch_fused_table(const TerrainDesc* tds, const int* tile0, int nterr, int total_tiles, int th, int* err,
+// k_hydro then k_transport over every tile of the batch's terrains; maps
+// holds MAPS_PER_TERRAIN tensor maps per terrain (device memory).
+void launch_fused_table(const BatchParams& bp, const CUtensorMap* maps, int total_tiles, int th, int* err,
                         cudaStream_t st);
 // Same for one terrain whose descriptor travels as a kernel parameter.
 void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st);

@@ -60,6 +60,8 @@ struct Tuning {
     int th = 0;  // 0: not tuned yet
     int graph = 0;
     double ms[4] = {};  // ms per step of (16, direct), (16, graph), (8, direct), (8, graph)
+    int per_world = 0;  // batches: each world's own launches were faster than one table launch
+    double ms_per_world = 0.0;
 };
 }  // namespace hg
 
@@ -114,9 +116,9 @@ struct Plan {
     std::vector<hg_world*> worlds;
     int th = 16;
     int total = 0;  // tiles over all terrains
-    TerrainDesc* d_tab[2] = {};
-    std::vector<TerrainDesc> h_tab[2];  // host copies (a single world launches from these)
-    int* d_tile0 = nullptr;
+    std::vector<TerrainDesc> h_tab[2];  // per direction; a single world launches from these
+    BatchParams* bp[2] = {};            // batch launches: terrain records (kernel parameter)
+    CUtensorMap* d_maps[2] = {};        // batch launches: tensor maps in device memory
     std::vector<std::array<const float*, S_COUNT>> key_cur, key_alt;  // buffers at build time
     std::vector<uint64_t> versions;
     cudaGraphExec_t graph[2] = {};  // two steps starting with table 0 / table 1
@@ -128,9 +130,10 @@ void destroy_plan(Plan*& p) {
     if (!p) return;
     for (auto& g : p->graph)
         if (g) cudaGraphExecDestroy(g);
-    cudaFree(p->d_tab[0]);
-    cudaFree(p->d_tab[1]);
-    cudaFree(p->d_tile0);
+    for (int d = 0; d < 2; ++d) {
+        cudaFree(p->d_maps[d]);
+        delete p->bp[d];
+    }
     delete p;
     p = nullptr;
 }
@@ -327,15 +330,23 @@ int build_plan(Plan* p) {
             if (!fill_desc(tab[i], s, p->th, tile0[i], w->tma))
                 return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a world buffer");
         }
-        if (!p->d_tab[dir]) HG_CUDA(cudaMalloc((void**)&p->d_tab[dir], sizeof(TerrainDesc) * nt));
-        HG_CUDA(cudaMemcpyAsync(p->d_tab[dir], tab.data(), sizeof(TerrainDesc) * nt, cudaMemcpyHostToDevice,
-                                p->stream));
-        HG_CUDA(cudaStreamSynchronize(p->stream));  // `tab` is reused for the other direction
         p->h_tab[dir] = tab;
+        if (nt > 1) {  // batch: records as a kernel parameter, tensor maps in device memory
+            if (!p->bp[dir]) p->bp[dir] = new BatchParams();
+            BatchParams& bp = *p->bp[dir];
+            bp.nterr = (int)nt;
+            std::vector<CUtensorMap> maps(nt * MAPS_PER_TERRAIN);
+            for (size_t i = 0; i < nt; ++i) {
+                bp.tile0[i] = tile0[i];
+                bp.t[i] = tab[i].h;
+                for (int m = 0; m < MAPS_PER_TERRAIN; ++m) maps[i * MAPS_PER_TERRAIN + m] = tab[i].maps[m];
+            }
+            if (!p->d_maps[dir]) HG_CUDA(cudaMalloc((void**)&p->d_maps[dir], sizeof(CUtensorMap) * maps.size()));
+            HG_CUDA(cudaMemcpyAsync(p->d_maps[dir], maps.data(), sizeof(CUtensorMap) * maps.size(),
+                                    cudaMemcpyHostToDevice, p->stream));
+            HG_CUDA(cudaStreamSynchronize(p->stream));  // `maps` is a local host buffer
+        }
     }
-    if (!p->d_tile0) HG_CUDA(cudaMalloc((void**)&p->d_tile0, sizeof(int) * nt));
-    HG_CUDA(cudaMemcpyAsync(p->d_tile0, tile0.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, p->stream));
-    HG_CUDA(cudaStreamSynchronize(p->stream));
     p->key_cur.resize(nt);
     p->key_alt.resize(nt);
     p->versions.resize(nt);
@@ -374,7 +385,7 @@ int plan_dir(const Plan* p) {
 // a kernel parameter, a batch launches over the device table.
 void launch_dir(Plan* p, int dir) {
     if (p->worlds.size() == 1) launch_fused_one(p->h_tab[dir][0], p->th, p->err, p->stream);
-    else launch_fused_table(p->d_tab[dir], p->d_tile0, (int)p->worlds.size(), p->total, p->th, p->err, p->stream);
+    else launch_fused_table(*p->bp[dir], p->d_maps[dir], p->total, p->th, p->err, p->stream);
 }
 
 // Brings a plan up to date (tables, device step counters, the graph that
@@ -837,6 +848,7 @@ int hg_batch_create(hg_world* const* worlds, int count, hg_batch** out) {
     if (!out) return fail(HG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (!worlds || count < 1) return fail(HG_ERR_INVALID, "a batch needs at least one world");
+    if (count > MAX_BATCH) return fail(HG_ERR_UNSUPPORTED, "a batch holds at most 128 worlds");
     for (int i = 0; i < count; ++i) {
         if (!worlds[i]) return fail(HG_ERR_INVALID, "null world in batch");
         if (worlds[i]->device != worlds[0]->device) return fail(HG_ERR_INVALID, "batch worlds must share a device");
@@ -889,16 +901,64 @@ int hg_batch_step(hg_batch* b, int nsteps, int mode) {
         }
         return HG_OK;
     }
-    // one table launch per kernel for every world: order after the worlds' streams
-    for (hg_world* w : b->worlds) {
-        HG_CUDA(cudaEventRecord(b->ev, w->stream));
-        HG_CUDA(cudaStreamWaitEvent(b->stream, b->ev, 0));
-    }
     const hg_step_options& o = b->worlds[0]->opt;
-    int rc = fused_run(b->plans, b->worlds, b->tuning, o.tile_y, o.graph, b->stream, b->err, nsteps);
-    HG_CUDA(cudaEventRecord(b->ev, b->stream));
-    for (hg_world* w : b->worlds) HG_CUDA(cudaStreamWaitEvent(w->stream, b->ev, 0));
-    return rc;
+    const bool autotune = o.tile_y == HG_AUTO && o.graph == HG_AUTO;
+    auto join_worlds = [&]() -> int {  // batch stream after every world's stream
+        for (hg_world* w : b->worlds) {
+            HG_CUDA(cudaEventRecord(b->ev, w->stream));
+            HG_CUDA(cudaStreamWaitEvent(b->stream, b->ev, 0));
+        }
+        return HG_OK;
+    };
+    auto release_worlds = [&]() -> int {  // every world's stream after the batch stream
+        HG_CUDA(cudaEventRecord(b->ev, b->stream));
+        for (hg_world* w : b->worlds) HG_CUDA(cudaStreamWaitEvent(w->stream, b->ev, 0));
+        return HG_OK;
+    };
+    auto per_world = [&](int k) -> int {
+        for (hg_world* w : b->worlds) {
+            int rc = hg_step(w, k, HG_MODE_FUSED);
+            if (rc != HG_OK) return rc;
+        }
+        return HG_OK;
+    };
+    if (autotune && b->tuning.th == 0 && nsteps >= 12) {
+        // Two untimed steps of per-world launches build (and capture) the
+        // worlds' own plans; the next two are timed.  fused_run then times the
+        // table variants; the faster form serves every later call.
+        cudaEvent_t e0, e1;
+        HG_CUDA(cudaEventCreate(&e0));
+        HG_CUDA(cudaEventCreate(&e1));
+        int rc = per_world(2);
+        if (rc == HG_OK) rc = join_worlds();
+        if (rc == HG_OK) rc = cudaEventRecord(e0, b->stream) == cudaSuccess ? release_worlds() : HG_ERR_CUDA;
+        if (rc == HG_OK) rc = per_world(2);
+        if (rc == HG_OK) rc = join_worlds();
+        if (rc == HG_OK && cudaEventRecord(e1, b->stream) != cudaSuccess) rc = HG_ERR_CUDA;
+        if (rc == HG_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = HG_ERR_CUDA;
+        float ms = 0;
+        if (rc == HG_OK) cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc != HG_OK) return rc == HG_ERR_CUDA ? cuda_fail(cudaGetLastError(), "batch tuning") : rc;
+        b->tuning.ms_per_world = ms / 2.0;
+        nsteps -= 4;
+        if ((rc = join_worlds()) != HG_OK) return rc;
+        rc = fused_run(b->plans, b->worlds, b->tuning, o.tile_y, o.graph, b->stream, b->err, 8);
+        if (rc != HG_OK) return rc;
+        nsteps -= 8;
+        double best = 1e30;
+        for (double m : b->tuning.ms) best = std::min(best, m);
+        b->tuning.per_world = b->tuning.ms_per_world < best ? 1 : 0;
+        if ((rc = release_worlds()) != HG_OK) return rc;
+    }
+    if (autotune && b->tuning.per_world) return per_world(nsteps);
+    // one table launch per kernel for every world: ordered after the worlds' streams
+    int rc = join_worlds();
+    if (rc != HG_OK) return rc;
+    rc = fused_run(b->plans, b->worlds, b->tuning, o.tile_y, o.graph, b->stream, b->err, nsteps);
+    int rc2 = release_worlds();
+    return rc != HG_OK ? rc : rc2;
 }
 
 int hg_batch_sync(hg_batch* b) {
@@ -930,6 +990,13 @@ int hg_batch_tuning(const hg_batch* b, int* tile_y, int* graph, double ms[4]) {
     if (graph) *graph = b->tuning.graph;
     if (ms)
         for (int k = 0; k < 4; ++k) ms[k] = b->tuning.ms[k];
+    return HG_OK;
+}
+
+int hg_batch_launch_form(const hg_batch* b, int* per_world, double* ms_per_world) {
+    if (!b) return fail(HG_ERR_INVALID, "null batch");
+    if (per_world) *per_world = b->tuning.per_world;
+    if (ms_per_world) *ms_per_world = b->tuning.ms_per_world;
     return HG_OK;
 }
 

@@ -108,6 +108,7 @@ def _load():
         "hg_batch_step": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
         "hg_batch_sync": (ctypes.c_int, [P]),
         "hg_batch_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
+        "hg_batch_launch_form": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
         "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_double)]),
         "hg_tape_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(P)]),
@@ -387,6 +388,13 @@ class Batch:
         th, g, ms = ctypes.c_int(), ctypes.c_int(), (ctypes.c_double * 4)()
         check(lib.hg_batch_tuning(self.h, ctypes.byref(th), ctypes.byref(g), ms))
         return th.value, g.value, list(ms)
+
+    def launch_form(self):
+        """(per_world, ms_per_world): 1 when the autotuner kept every world's
+        own launches over one table launch."""
+        pw, ms = ctypes.c_int(), ctypes.c_double()
+        check(lib.hg_batch_launch_form(self.h, ctypes.byref(pw), ctypes.byref(ms)))
+        return pw.value, ms.value
 
 
 def config3_terrains(count=64, seed=0):

@@ -227,6 +227,12 @@ int hg_batch_step(hg_batch* b, int nsteps, int mode);
 int hg_batch_sync(hg_batch* b);
 int hg_batch_stream(const hg_batch* b, void** stream);
 int hg_batch_tuning(const hg_batch* b, int* tile_y, int* graph, double ms[4]);
+/* Launch form HG_MODE_FUSED chose: with tile_y and graph at HG_AUTO, the first
+ * HG_MODE_FUSED call of at least 12 steps also times two steps of every
+ * world's own fused launches (4 steps: 2 untimed, 2 timed) and keeps that
+ * form when it beat the fastest table launch (per_world 1).  ms_per_world is
+ * its ms per step (0 before tuning). */
+int hg_batch_launch_form(const hg_batch* b, int* per_world, double* ms_per_world);
 
 /* FP64 totals over the grid, computed on the device:
  * out[0] rock, out[1] water, out[2] sediment.  Synchronises. */

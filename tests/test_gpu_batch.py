@@ -78,16 +78,22 @@ def test_autotuner_picks_a_variant_and_keeps_results():
     ts = terrains()
     ref = make(ts)
     for w in ref:
-        w.step(20, H.MODE_PLAIN)
+        w.step(27, H.MODE_PLAIN)
     ws = make(ts)
     b = H.Batch(ws)
-    b.step(20, H.MODE_FUSED)  # first 8 steps time the four variants
+    b.step(20, H.MODE_FUSED)  # first 12 steps time per-world launches and the four table variants
     b.sync()
     th, graph, ms = b.tuning()
     assert th in (16, 8) and graph in (0, 1)
     assert all(m > 0 for m in ms)
+    per_world, ms_pw = b.launch_form()
+    assert per_world in (0, 1) and ms_pw > 0
+    assert per_world == (ms_pw < min(ms))
+    b.step(7, H.MODE_FUSED)  # the chosen form
+    b.sync()
     for a, c in zip(ref, ws):
         same(a, c)
+        assert c.step_count == 27
 
 
 def test_world_autotune_and_settings_change_rebuilds_tables():
