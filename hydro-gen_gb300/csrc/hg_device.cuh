@@ -44,14 +44,38 @@ __device__ __forceinline__ float poly_atan_core(float u) {
     p = __fadd_rn(__fmul_rn(p, s), c0);
     return __fadd_rn(u, __fmul_rn(u, __fmul_rn(s, p)));
 }
+// The three branches share one division and one polynomial evaluation
+// (lanes of a warp taking different branches do not repeat them).
 __device__ __forceinline__ float poly_atanf(float x) {
-    float ax = fabsf(x), r;
-    if (ax <= 0.414213562f) r = poly_atan_core(ax);
-    else if (ax <= 2.41421356f)
-        r = __fadd_rn(0.785398163f, poly_atan_core(__fdiv_rn(__fsub_rn(ax, 1.0f), __fadd_rn(ax, 1.0f))));
-    else r = __fsub_rn(1.57079637f, poly_atan_core(__fdiv_rn(1.0f, ax)));
+    const float ax = fabsf(x);
+    const bool mid = ax > 0.414213562f && ax <= 2.41421356f;
+    const bool big = ax > 2.41421356f;
+    float u = ax;
+    if (mid || big) u = __fdiv_rn(mid ? __fsub_rn(ax, 1.0f) : 1.0f, mid ? __fadd_rn(ax, 1.0f) : ax);
+    const float p = poly_atan_core(u);
+    float r = p;
+    if (mid) r = __fadd_rn(0.785398163f, p);
+    else if (big) r = __fsub_rn(1.57079637f, p);
     return copysignf(r, x);
 }
+
+// Correctly rounded a / b from y = RN(1/b), two correction steps after the
+// product a*y (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Develop. 34(1), 1990): q0 = RN(a*y)
+// lies within 2 ulp of a/b, the first correction brings it within 1 ulp, and
+// with y within half an ulp of 1/b Markstein's theorem makes the second
+// correction the correctly rounded quotient.  Holds while no product
+// overflows and no residual underflows: callers keep a at 0 or in
+// [2^-80, 2^80] and b in [2^-30, 2^40].
+__device__ __forceinline__ float div_recip(float a, float b, float y) {
+    float q = __fmul_rn(a, y);
+    float r = __fmaf_rn(-q, b, a);
+    q = __fmaf_rn(r, y, q);
+    r = __fmaf_rn(-q, b, a);
+    return __fmaf_rn(r, y, q);
+}
+constexpr float SQRT2_F = 1.41421354f;
+constexpr float RCP_SQRT2_F = 0x1.6a09e6p-1f;  // RN(1 / SQRT2_F)
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers:
 // as easy as 1, 2, 3", SC'11) ---------------------------------------------------
@@ -102,8 +126,9 @@ struct StepConsts {
     float evap;           // 1 - Ke*d_t
     float Kalpha0, Kspeed0;
     int thermal;          // thermal layer-0 passes enabled (Kspeed[0] != 0)
-    float talus_x_cross;  // smallest slope whose poly_atanf exceeds Kalpha0
-    float talus_b_diag;   // smallest height drop whose diagonal slope does
+    float talus_x_cross;  // smallest positive slope whose poly_atanf exceeds Kalpha0
+    float talus_b_diag;   // smallest positive height drop whose diagonal slope does
+    int fast_div;         // both thresholds >= 2^-30: outflow quotients by div_recip
 };
 
 // ---- hydro_flux, glsl/hydro_flux.glsl:77-166 -------------------------------------
@@ -264,12 +289,16 @@ __device__ __forceinline__ ThermalOut cell_thermal_ref(const StepConsts& c, floa
     return o;
 }
 
-// Same result with one arctangent per cell.  poly_atanf is monotone
-// non-decreasing on x >= 0 (checked over every positive float), so
-// "poly_atanf(slope) > Kalpha0" is "slope >= talus_x_cross" (diagonal:
-// "drop >= talus_b_diag", division rounding being monotone too), and the
-// largest marked sharpness is that of the steepest marked slope.
-__device__ __forceinline__ ThermalOut cell_thermal_fast(const StepConsts& c, float b, const float nb[8]) {
+// The shader's outflows with one arctangent per cell, written to o[8].
+// poly_atanf is monotone non-decreasing on x >= 0 (checked over every
+// positive float), so "poly_atanf(slope) > Kalpha0" is "slope >=
+// talus_x_cross" (diagonal: "drop >= talus_b_diag", division rounding being
+// monotone too; both thresholds are positive, so a marked drop is > 0), and
+// the largest marked sharpness is that of the steepest marked slope.  The
+// quotients S*dh/bk share their divisor: with the operands in div_recip's
+// range they come from one reciprocal, else from IEEE division; either way
+// they are the correctly rounded quotients of the shader's expression.
+__device__ __forceinline__ void cell_thermal_outflows(const StepConsts& c, float b, const float nb[8], float o[8]) {
     float dh[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];
@@ -278,29 +307,40 @@ __device__ __forceinline__ ThermalOut cell_thermal_fast(const StepConsts& c, flo
     for (int k = 0; k < 8; ++k)
         if (dh[k] > H) H = dh[k];
     H = gmin(b, H);
-    ThermalOut o{0.0f, 0.0f, 0u};
-    float max_cross = 0.0f, max_diag = 0.0f;
+    float bk = 0.0f, max_cross = 0.0f, max_diag = 0.0f;
+    bool mk[8], any = false;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        float bb = dh[k];
-        bool marked = k < 4 ? (bb >= c.talus_x_cross) : (bb >= c.talus_b_diag);
-        if (bb > 0.0f && marked) {
-            o.bk += bb;
-            o.mask |= 1u << k;
-            if (k < 4) max_cross = fmaxf(max_cross, bb);
-            else max_diag = fmaxf(max_diag, bb);
+        mk[k] = dh[k] >= (k < 4 ? c.talus_x_cross : c.talus_b_diag);
+        if (mk[k]) {
+            bk += dh[k];
+            any = true;
+            if (k < 4) max_cross = fmaxf(max_cross, dh[k]);
+            else max_diag = fmaxf(max_diag, dh[k]);
         }
     }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o[k] = 0.0f;
+    if (!any) return;
+    bool fast = c.fast_div && bk <= 0x1p40f;  // then max_diag is 0 or in [2^-30, 2^40]
+    const float sd = fast ? div_recip(max_diag, SQRT2_F, RCP_SQRT2_F) : max_diag / SQRT2_F;
+    const float alph = poly_atanf(fmaxf(max_cross, sd));
     float sharp = 1.0f;
-    if (o.mask) {
-        float slope = fmaxf(max_cross, max_diag / 1.41421354f);
-        float alph = poly_atanf(slope);
-        float newsh = 1.0f + alph - c.Kalpha0;
-        if (newsh > sharp) sharp = newsh;
-    }
+    const float newsh = 1.0f + alph - c.Kalpha0;
+    if (newsh > sharp) sharp = newsh;
     sharp *= sharp * sharp;
-    o.S = c.dt * c.Kspeed0 * sharp * H / 2.0f;
-    return o;
+    const float S = c.dt * c.Kspeed0 * sharp * H / 2.0f;  // a == L == 1
+    fast = fast && S >= 0x1p-50f && S <= 0x1p40f;
+    if (fast) {
+        const float y = __frcp_rn(bk);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (mk[k]) o[k] = div_recip(S * dh[k], bk, y);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (mk[k]) o[k] = S * dh[k] / bk;
+    }
 }
 
 // ---- thermal_transport (layer 0), glsl/thermal_transport.glsl:31-65 ----------------

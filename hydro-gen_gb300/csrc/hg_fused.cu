@@ -255,9 +255,7 @@ __device__ __forceinline__ void outflows_scalar(const StepConsts& c, const float
         }
         nb[d] = out ? FAR_HEIGHT : be[si + f_oy[d] * RW + f_ox[d]];
     }
-    ThermalOut t = cell_thermal_fast(c, b, nb);
-#pragma unroll
-    for (int d = 0; d < 8; ++d) o8[d] = (t.mask >> d & 1u) ? t.S * (b - nb[d]) / t.bk : 0.0f;
+    cell_thermal_outflows(c, b, nb, o8);
 }
 
 template <int TH, bool EDGE>
@@ -325,10 +323,10 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
             nb[5] = (has_r && has_t) ? (j == 3 ? pr : at4(p4, j + 1)) : FAR_HEIGHT;
             nb[6] = (has_l && has_b) ? (j == 0 ? ml : at4(m4, j - 1)) : FAR_HEIGHT;
             nb[7] = (has_r && has_b) ? (j == 3 ? mr : at4(m4, j + 1)) : FAR_HEIGHT;
-            const float b = at4(c4, j);
-            ThermalOut t = cell_thermal_fast(c, b, nb);
+            float o8[8];
+            cell_thermal_outflows(c, at4(c4, j), nb, o8);
 #pragma unroll
-            for (int d = 0; d < 8; ++d) o[d][j] = (t.mask >> d & 1u) ? t.S * (b - nb[d]) / t.bk : 0.0f;
+            for (int d = 0; d < 8; ++d) o[d][j] = o8[d];
         }
         const int oi = (ry - 1) * RW + rx0;
 #pragma unroll

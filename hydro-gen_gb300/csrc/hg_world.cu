@@ -13,6 +13,8 @@
 #include <vector>
 #include <string>
 
+#include <limits>
+
 #include "hg_internal.h"
 
 namespace hg {
@@ -259,6 +261,12 @@ StepConsts make_consts(const hg_world* w) {
     c.thermal = thermal_on(w) ? 1 : 0;
     c.talus_x_cross = talus_cross_threshold(s.Kalpha[0]);
     c.talus_b_diag = talus_diag_threshold(c.talus_x_cross);
+    // a marked drop is also > 0: fold that into the thresholds (the smallest
+    // positive float is the first drop > 0)
+    const float tiny = std::numeric_limits<float>::denorm_min();
+    if (c.talus_x_cross < tiny) c.talus_x_cross = tiny;
+    if (c.talus_b_diag < tiny) c.talus_b_diag = tiny;
+    c.fast_div = !(c.talus_x_cross < 0x1p-30f) && !(c.talus_b_diag < 0x1p-30f);
     return c;
 }
 

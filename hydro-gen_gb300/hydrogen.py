@@ -108,6 +108,7 @@ def _load():
         "hg_batch_step": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
         "hg_batch_sync": (ctypes.c_int, [P]),
         "hg_batch_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
+        "hg_selftest_division": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
         "hg_batch_launch_form": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
         "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_double)]),

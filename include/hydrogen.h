@@ -299,6 +299,13 @@ int hg_world_load(hg_world* w, const char* path);
 #define HG_NOALLOC_MAX_FIELDS 8
 int hg_field_totals_noalloc(const float* const* fields, int nfields, size_t count, double* out, void* stream);
 
+/* ---- self-tests ------------------------------------------------------------------------- */
+/* No counterpart in the reference.  Draws `count` operand pairs (seeded) in
+ * the range where the fused kernel divides through a shared reciprocal
+ * (Markstein's correction) and counts results that differ in any bit from
+ * IEEE division; 0 is the only passing answer.  Synchronises. */
+int hg_selftest_division(uint64_t seed, uint64_t count, uint64_t* mismatches);
+
 #ifdef __cplusplus
 }
 #endif

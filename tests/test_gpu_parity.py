@@ -238,3 +238,12 @@ def test_minimum_grid():
     w.step(20, H.MODE_PLAIN)
     ow.step(s, o, 20)
     assert_bitwise(w, ow)
+
+
+def test_shared_reciprocal_division_is_ieee_division():
+    """The fused talus kernel divides S*dh by bk through one reciprocal and
+    Markstein's correction; every bit must match IEEE division."""
+    import ctypes
+    bad = ctypes.c_uint64()
+    H.check(H.lib.hg_selftest_division(12345, 1 << 30, ctypes.byref(bad)))
+    assert bad.value == 0
