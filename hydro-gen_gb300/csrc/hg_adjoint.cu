@@ -1,27 +1,38 @@
 // Reverse-mode adjoint of the grid step without thermal erosion.
 //
-// One reversed step works on the step's input state X (restored from a
-// checkpoint and recomputed) and the adjoint A of its outputs:
-//   k_adj_recompute  rain, flux and erosion of every cell (the forward cell
-//                    code of hg_device.cuh, so the intermediates are the
-//                    forward's own bits): water after rain, u, v, d1+d2, d2,
-//                    eroded rock and sediment
-//   k_adj_sediment   semi-Lagrangian gather reversed: each cell scatters its
-//                    sediment adjoint to its four taps (atomicAdd: the taps
-//                    of a back-trace are data dependent), and the velocity
-//                    adjoint of the back-trace point
-//   k_adj_erosion    dissolve/deposit/exhaustion branch reversed; the
-//                    terrain normal's neighbour terms become per-cell
-//                    packets; per-cell Ks gradient accumulated
-//   k_adj_flux       outflow, scaling, water update and velocity reversed;
-//                    neighbour terms become per-cell packets
-//   k_adj_gather     every cell sums its own terms and its neighbours'
-//                    packets into the input adjoint (deterministic order)
+// One reversed step j works on the step's input state X_j, the step's
+// forward intermediates kept by the segment recompute (velocity u, v and the
+// eroded sediment se of every cell: the fused forward step writes them
+// anyway) and the adjoint A of the step's outputs.  The adjoint of a state is
+// kept as each cell's own terms plus ten packet fields that carry the terms
+// of its neighbours' inputs; a reader adds the neighbours' packets in a
+// fixed order (deterministic), so no separate gather pass runs.  One kernel
+// per step:
+//   k_adj_cell      TMA-staged 64 x 4 tiles of X_j with a one-cell halo,
+//                   this step's rain added in shared memory; one thread per
+//                   cell gathers the cell's adjoint inputs while the tile
+//                   flies, recomputes the forward flux and erosion (the
+//                   operations of hg_device.cuh, so every branch is the
+//                   forward's) and reverses them; it writes its own terms
+//                   and packets, accumulates the Ks gradient and clears its
+//                   sediment-adjoint cell (double buffer); then, with the
+//                   cell's sediment adjoint of step j - 1 now final, it
+//                   reverses that step's semi-Lagrangian gather: a scatter
+//                   to the back-trace's four taps (atomicAdd: the taps are
+//                   data dependent) and the back-trace velocity adjoint
+//   k_adj_sediment  the same scatter on its own, for a segment's last step
+//                   (its intermediates exist only after the recompute)
+//   k_adj_final     the gathered rock adjoint of the first state
+//
 // Subgradients: max(0, x) and min(1, q) pass the derivative of the taken
 // argument (ties take the constant side), clamps pass 0 when clamped,
 // dissolve/deposit/exhaustion use the taken branch, floor() is locally
-// constant.  The formulas follow the shaders cited in hg_device.cuh.
+// constant.  The formulas follow the shaders cited in hg_device.cuh.  The
+// reversed arithmetic divides through correctly rounded reciprocals
+// (x * (1/y), within two ulps of x / y); the recomputed forward keeps IEEE
+// division, so its values and branches are the forward's own.
 #include "hg_internal.h"
+#include "hg_tma.cuh"
 
 namespace hg {
 
@@ -30,73 +41,20 @@ namespace {
 constexpr int BX = 32, BY = 8;
 __device__ __forceinline__ size_t at(int n, int x, int y) { return (size_t)y * n + x; }
 
-// water after this step's rain
-__global__ void k_adj_rain(StepConsts c, RainStep r, const float* __restrict__ d, float* __restrict__ dr) {
-    int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x0 >= c.n || y >= c.n) return;
-    size_t i = at(c.n, x0, y);
-    float4 v = *reinterpret_cast<const float4*>(d + i);
-    if (r.active) {
-        uint32_t w[4] = {0, 0, 0, 0};
-        if (r.bernoulli) rain_words4(r, x0, y, w);
-        v.x += rain_incr(r, w[0]);
-        v.y += rain_incr(r, w[1]);
-        v.z += rain_incr(r, w[2]);
-        v.w += rain_incr(r, w[3]);
-    }
-    *reinterpret_cast<float4*>(dr + i) = v;
-}
-
-__global__ void k_adj_recompute(StepConsts c, AdjFields X, AdjTemps T) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
+// ---- sediment_transport reversed ------------------------------------------------
+// Cell (x, y) of a step whose output sediment adjoint is `a`: scatter to the
+// back-trace taps of dse, back-trace velocity adjoint into du, dv.
+__device__ __forceinline__ void sediment_adjoint(const StepConsts& c, const AdjSlot& sl, int x, int y, size_t i,
+                                                 float a, float* dse, float* du, float* dv) {
     const int n = c.n;
-    if (x >= n || y >= n) return;
-    size_t i = at(n, x, y);
-    auto w = [&](int xx, int yy) -> float {
-        if (xx < 0 || xx >= n || yy < 0 || yy >= n) return FAR_HEIGHT;
-        size_t j = at(n, xx, yy);
-        return X.b[j] + T.dr[j];
-    };
-    float d1 = T.dr[i];
-    float inl = x > 0 ? X.f[1][i - 1] : 0.0f;
-    float inr = x < n - 1 ? X.f[0][i + 1] : 0.0f;
-    float int_ = y < n - 1 ? X.f[3][i + n] : 0.0f;
-    float inb = y > 0 ? X.f[2][i - n] : 0.0f;
-    FluxOut o = cell_flux(c, x, y, X.b[i] + d1, d1, X.f[0][i], X.f[1][i], X.f[2][i], X.f[3][i], w(x - 1, y),
-                          w(x + 1, y), w(x, y + 1), w(x, y - 1), inl, inr, int_, inb);
-    float b = X.b[i], s = X.s[i];
-    float br = x < n - 1 ? X.b[i + 1] : 0.0f, bl = x > 0 ? X.b[i - 1] : 0.0f;
-    float bb = y > 0 ? X.b[i - n] : 0.0f, bt = y < n - 1 ? X.b[i + n] : 0.0f;
-    float Kls0 = c.ks_field ? c.dt * c.ks_field[i] : c.Kls0;
-    cell_erosion(c, Kls0, o.u, o.v, o.vz, b, s, br, bl, bb, bt);
-    T.u[i] = o.u;
-    T.v[i] = o.v;
-    T.vz[i] = o.vz;
-    T.d2[i] = o.d2;
-    T.be[i] = b;
-    T.se[i] = s;
-}
-
-__global__ void k_adj_sediment(StepConsts c, AdjFields A, AdjTemps T, AdjWork W) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int n = c.n;
-    if (x >= n || y >= n) return;
-    size_t i = at(n, x, y);
-    W.dd2[i] = A.d[i] * c.evap;
-    const float a = A.s[i];
     const float maxc = (float)(n - 1);
-    float rx = (float)x - T.u[i] * c.dt, ry = (float)y - T.v[i] * c.dt;
+    float rx = (float)x - sl.u[i] * c.dt, ry = (float)y - sl.v[i] * c.dt;
     float px = gclamp(rx, 0.0f, maxc), py = gclamp(ry, 0.0f, maxc);
     int ix = min(max((int)px, 0), n - 1), iy = min(max((int)py, 0), n - 1);
     float fx = px - floorf(px), fy = py - floorf(py);
-    auto S = [&](int xx, int yy) -> float {
-        return (xx < n && yy < n) ? T.se[at(n, xx, yy)] : 0.0f;
-    };
+    auto S = [&](int xx, int yy) -> float { return (xx < n && yy < n) ? sl.se[at(n, xx, yy)] : 0.0f; };
     auto add = [&](int xx, int yy, float v) {
-        if (xx < n && yy < n && v != 0.0f) atomicAdd(W.dse + at(n, xx, yy), v);
+        if (xx < n && yy < n && v != 0.0f) atomicAdd(dse + at(n, xx, yy), v);
     };
     add(ix, iy, a * (1.0f - fx) * (1.0f - fy));
     add(ix + 1, iy, a * fx * (1.0f - fy));
@@ -105,177 +63,312 @@ __global__ void k_adj_sediment(StepConsts c, AdjFields A, AdjTemps T, AdjWork W)
     float s00 = S(ix, iy), s10 = S(ix + 1, iy), s01 = S(ix, iy + 1), s11 = S(ix + 1, iy + 1);
     float dfx = (s10 - s00) * (1.0f - fy) + (s11 - s01) * fy;
     float dfy = (s01 * (1.0f - fx) + s11 * fx) - (s00 * (1.0f - fx) + s10 * fx);
-    W.du[i] = (rx > 0.0f && rx < maxc) ? a * dfx * (-c.dt) : 0.0f;
-    W.dv[i] = (ry > 0.0f && ry < maxc) ? a * dfy * (-c.dt) : 0.0f;
+    du[i] = (rx > 0.0f && rx < maxc) ? a * dfx * (-c.dt) : 0.0f;
+    dv[i] = (ry > 0.0f && ry < maxc) ? a * dfy * (-c.dt) : 0.0f;
 }
 
-__global__ void k_adj_erosion(StepConsts c, AdjFields X, AdjFields A, AdjTemps T, AdjWork W, float* __restrict__ dks) {
+__global__ void k_adj_sediment(StepConsts c, AdjSlot sl, const float* __restrict__ as_, float* __restrict__ dse,
+                               float* __restrict__ du, float* __restrict__ dv) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int n = c.n;
-    if (x >= n || y >= n) return;
-    size_t i = at(n, x, y);
-    auto B = [&](int xx, int yy) -> float {
-        return (xx < 0 || xx >= n || yy < 0 || yy >= n) ? 0.0f : X.b[at(n, xx, yy)];
-    };
-    float u = T.u[i], v = T.v[i], vz = T.vz[i];
-    float len = sqrtf(u * u + v * v), ero = len, dero_dlen = 1.0f, dero_dvz = 0.0f;
-    if (vz < 1e-3f) {
-        float dd = gmax(5e-4f, vz);
-        float tr = (dd - 1e-3f) / (5e-4f - 1e-3f);
-        float t = gclamp(tr, 0.0f, 1.0f);
-        float sm = t * t * (3.0f - 2.0f * t);
-        ero = len * (1.0f - sm);
-        dero_dlen = 1.0f - sm;
-        if (vz > 5e-4f && tr > 0.0f && tr < 1.0f) dero_dvz = -len * 6.0f * t * (1.0f - t) / (5e-4f - 1e-3f);
-    }
-    float dx = B(x + 1, y) - B(x - 1, y), dz = B(x, y + 1) - B(x, y - 1);
-    float L3 = sqrtf(4.0f * dx * dx + 16.0f + 4.0f * dz * dz);
-    float ny = -4.0f / L3;
-    float sin_a = sqrtf(1.0f - ny * ny);
-    float sa = gmax(0.02f, sin_a);
-    float craw = c.Kc * sa * ero;
-    float cc = gmax(0.0f, craw);
-    float Ks_i = c.ks_field ? c.ks_field[i] : c.Ks0;
-    float Kls = c.dt * Ks_i, Kld = c.Kld0, b = X.b[i], s = X.s[i];
-    float ab = A.b[i], as = W.dse[i];
-    float gb, gs, gc = 0.0f, gK = 0.0f;
-    if (cc > s) {
-        float del = Kls * (cc - s);
-        if (b - del < 0.0f) {  // rock exhausted: b' = 0, s' = s + b
-            gb = as;
-            gs = as;
-        } else {
-            gb = ab;
-            gs = ab * Kls + as * (1.0f - Kls);
-            gc = (as - ab) * Kls;
-            gK = (as - ab) * (cc - s);
-        }
-    } else {
-        gb = ab;
-        gs = ab * Kld + as * (1.0f - Kld);
-        gc = (as - ab) * Kld;
-    }
-    dks[i] += gK * c.dt;
-    W.rb[i] = gb;
-    W.rs[i] = gs;
-    float pdx = 0.0f, pdz = 0.0f, du = 0.0f, dv = 0.0f, dvz = 0.0f;
-    if (craw > 0.0f) {
-        float gsa = gc * c.Kc * ero, gero = gc * c.Kc * sa;
-        if (sin_a > 0.02f) {
-            float gny = gsa * (-ny / sin_a);
-            float gL3 = gny * (4.0f / (L3 * L3));
-            pdx = gL3 * 4.0f * dx / L3;
-            pdz = gL3 * 4.0f * dz / L3;
-        }
-        float glen = gero * dero_dlen;
-        dvz = gero * dero_dvz;
-        if (len > 0.0f) {
-            du = glen * u / len;
-            dv = glen * v / len;
-        }
-    }
-    W.pdx[i] = pdx;
-    W.pdz[i] = pdz;
-    W.du[i] += du;
-    W.dv[i] += dv;
-    W.dvz[i] = dvz;
+    if (x >= c.n || y >= c.n) return;
+    size_t i = at(c.n, x, y);
+    sediment_adjoint(c, sl, x, y, i, as_[i], dse, du, dv);
 }
 
-__global__ void k_adj_flux(StepConsts c, AdjFields X, AdjFields A, AdjTemps T, AdjWork W) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int n = c.n;
-    if (x >= n || y >= n) return;
-    size_t i = at(n, x, y);
-    const int ox[4] = {-1, 1, 0, 0}, oy[4] = {0, 0, 1, -1};
-    auto w = [&](int xx, int yy) -> float {
-        if (xx < 0 || xx >= n || yy < 0 || yy >= n) return FAR_HEIGHT;
-        size_t j = at(n, xx, yy);
-        return X.b[j] + T.dr[j];
-    };
-    const float d1 = T.dr[i], wc = X.b[i] + d1;
-    float ft[4], g[4];
-    bool live[4];
-    for (int k = 0; k < 4; ++k) {
-        ft[k] = c.EK * X.f[k][i] + c.dt * (c.G * (wc - w(x + ox[k], y + oy[k])));
-        g[k] = gmax(0.0f, ft[k]);
-        live[k] = ft[k] > 0.0f;
-    }
-    if (x <= 0) { g[0] = 0.0f; live[0] = false; } else if (x >= n - 1) { g[1] = 0.0f; live[1] = false; }
-    if (y <= 0) { g[3] = 0.0f; live[3] = false; } else if (y >= n - 1) { g[2] = 0.0f; live[2] = false; }
-    float inl = x > 0 ? X.f[1][i - 1] : 0.0f, inr = x < n - 1 ? X.f[0][i + 1] : 0.0f;
-    float it = y < n - 1 ? X.f[3][i + n] : 0.0f, ib = y > 0 ? X.f[2][i - n] : 0.0f;
-    float sum_in = inl + inr + it + ib;
-    float sum_out = g[0] + g[1] + g[2] + g[3];
-    float den = sum_out * c.dt;
-    bool scaled = !(d1 >= den) && (d1 / den) < 1.0f;  // K = d1/den (else K = 1)
-    float K = scaled ? d1 / den : 1.0f;
-    float arg = d1 + c.dt * (sum_in - sum_out * K);
-    float vz = T.vz[i], u = T.u[i], v = T.v[i];
-    float gvz = W.dvz[i], gin[4] = {0, 0, 0, 0}, gfown[4] = {0, 0, 0, 0};
-    if (vz > 0.0f) {
-        float du = W.du[i] / vz, dv = W.dv[i] / vz;
-        gin[0] += du; gin[1] -= du;
-        gfown[0] -= du; gfown[1] += du;
-        gin[3] += dv; gin[2] -= dv;
-        gfown[3] -= dv; gfown[2] += dv;
-        gvz -= (W.du[i] * u + W.dv[i] * v) / vz;
-    }
-    float gd1 = gvz, gd2 = gvz + W.dd2[i];
-    float garg = arg > 0.0f ? gd2 : 0.0f;
-    gd1 += garg;
-    float gsum_in = c.dt * garg, gsum_outK = -c.dt * garg;
-    for (int k = 0; k < 4; ++k) gin[k] += gsum_in;
-    float gK = gsum_outK * sum_out, gsum_out = gsum_outK * K;
-    for (int k = 0; k < 4; ++k) gK += A.f[k][i] * g[k];
-    float gg[4];
-    for (int k = 0; k < 4; ++k) gg[k] = A.f[k][i] * K + gsum_out;
-    if (scaled) {
-        gd1 += gK / den;
-        float gden = -gK * d1 / (den * den);
-        for (int k = 0; k < 4; ++k) gg[k] += gden * c.dt;
-    }
-    float gw = 0.0f;
-    for (int k = 0; k < 4; ++k) {
-        float gdh = 0.0f;
-        if (live[k]) {
-            gfown[k] += c.EK * gg[k];
-            gdh = c.dt * c.G * gg[k];
-            gw += gdh;
-        }
-        W.pdh[k][i] = gdh;
-        W.pin[k][i] = gin[k];
-        W.fown[k][i] = gfown[k];
-    }
-    W.wbar[i] = gw;
-    W.gd1[i] = gd1;
-}
-
-__global__ void k_adj_gather(int n, AdjWork W, AdjFields R) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= n || y >= n) return;
-    size_t i = at(n, x, y);
+// Gathered adjoint of a state at cell i: own terms plus the neighbours'
+// packets (L, R, T, B neighbours, fixed order).
+__device__ __forceinline__ void adj_view_at(const AdjView& A, int n, int x, int y, size_t i, float& ab, float& ad,
+                                            float af[4]) {
     // w = rock + water: a neighbour's height difference toward this cell
     // (its direction opposite to ours) enters with a minus sign
     float nbw = 0.0f;
-    if (x > 0) nbw += W.pdh[1][i - 1];      // left neighbour's R
-    if (x < n - 1) nbw += W.pdh[0][i + 1];  // right neighbour's L
-    if (y < n - 1) nbw += W.pdh[3][i + n];  // top neighbour's B
-    if (y > 0) nbw += W.pdh[2][i - n];      // bottom neighbour's T
+    if (x > 0) nbw += A.pdh[1][i - 1];      // left neighbour's R
+    if (x < n - 1) nbw += A.pdh[0][i + 1];  // right neighbour's L
+    if (y < n - 1) nbw += A.pdh[3][i + n];  // top neighbour's B
+    if (y > 0) nbw += A.pdh[2][i - n];      // bottom neighbour's T
     float nrm = 0.0f;  // terrain-normal terms of the neighbours
-    if (x > 0) nrm += W.pdx[i - 1];
-    if (x < n - 1) nrm -= W.pdx[i + 1];
-    if (y > 0) nrm += W.pdz[i - n];
-    if (y < n - 1) nrm -= W.pdz[i + n];
-    R.b[i] = W.rb[i] + W.wbar[i] - nbw + nrm;
-    R.d[i] = W.wbar[i] + W.gd1[i] - nbw;
-    R.s[i] = W.rs[i];
-    R.f[0][i] = W.fown[0][i] + (x > 0 ? W.pin[1][i - 1] : 0.0f);      // left neighbour's inflow from me
-    R.f[1][i] = W.fown[1][i] + (x < n - 1 ? W.pin[0][i + 1] : 0.0f);  // right neighbour's inflow from me
-    R.f[2][i] = W.fown[2][i] + (y < n - 1 ? W.pin[3][i + n] : 0.0f);  // top neighbour's inflow from me
-    R.f[3][i] = W.fown[3][i] + (y > 0 ? W.pin[2][i - n] : 0.0f);      // bottom neighbour's inflow from me
+    if (x > 0) nrm += A.pdx[i - 1];
+    if (x < n - 1) nrm -= A.pdx[i + 1];
+    if (y > 0) nrm += A.pdz[i - n];
+    if (y < n - 1) nrm -= A.pdz[i + n];
+    ab = (A.b[i] - nbw) + nrm;
+    ad = A.d[i] - nbw;
+#pragma unroll
+    for (int d = 0; d < 4; ++d) af[d] = A.f[d][i];
+    if (x > 0) af[0] += A.pin[1][i - 1];      // left neighbour's inflow from me
+    if (x < n - 1) af[1] += A.pin[0][i + 1];  // right neighbour's inflow from me
+    if (y < n - 1) af[2] += A.pin[3][i + n];  // top neighbour's inflow from me
+    if (y > 0) af[3] += A.pin[2][i - n];      // bottom neighbour's inflow from me
+}
+
+// ---- k_adj_cell ------------------------------------------------------------------
+constexpr int TW = 64, TH = 4, HX = 4, RW = TW + 2 * HX, NTH = TW * TH;
+constexpr int H_RH = TH + 2, H_BOX = RW * H_RH, H_RC = ((H_BOX + 31) / 32) * 32;
+enum { X_B = 0, X_D, X_S, X_FL, X_FR, X_FT, X_FB, X_N };
+
+// Forward flux of one cell with the intermediates its adjoint needs: the
+// operations of cell_flux (hg_device.cuh), so every branch is the forward's.
+// Directions L, R, T, B; wn[] neighbour totals, in[] neighbours' facing flux.
+struct FluxFwd {
+    float g[4];
+    bool live[4];
+    float sum_out, den, K, arg, vz, u, v;
+    bool scaled;
+};
+__device__ __forceinline__ FluxFwd flux_fwd(const StepConsts& c, int x, int y, float w_c, float d1, const float f[4],
+                                            const float wn[4], const float in[4], bool border) {
+    FluxFwd o;
+    float ft[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        ft[k] = c.EK * f[k] + c.dt * (c.G * (w_c - wn[k]));
+        o.g[k] = gmax(0.0f, ft[k]);
+        o.live[k] = ft[k] > 0.0f;
+    }
+    if (border) {
+        if (x <= 0) { o.g[0] = 0.0f; o.live[0] = false; }
+        else if (x >= c.n - 1) { o.g[1] = 0.0f; o.live[1] = false; }
+        if (y <= 0) { o.g[3] = 0.0f; o.live[3] = false; }
+        else if (y >= c.n - 1) { o.g[2] = 0.0f; o.live[2] = false; }
+    }
+    float sum_in = in[0] + in[1] + in[2] + in[3];
+    o.sum_out = o.g[0] + o.g[1] + o.g[2] + o.g[3];
+    o.den = o.sum_out * c.dt;
+    o.scaled = false;
+    o.K = 1.0f;
+    if (!(d1 >= o.den)) {
+        float q = d1 / o.den;
+        if (q < 1.0f) { o.scaled = true; o.K = q; }
+    }
+    o.arg = d1 + c.dt * (sum_in - o.sum_out * o.K);
+    float d2 = gmax(0.0f, o.arg);
+    o.vz = d1 + d2;
+    if (o.vz > 0.0f) {
+        o.u = (in[0] - f[0] + f[1] - in[1]) / o.vz;
+        o.v = (in[3] - f[3] + f[2] - in[2]) / o.vz;
+    } else {
+        o.u = 0.0f; o.v = 0.0f;
+    }
+    return o;
+}
+
+template <bool EDGE>
+__device__ __forceinline__ void adj_tile(const AdjCellArgs& a, float* sm, uint64_t* bar, int tx0, int ty0,
+                                         int* err) {
+    const StepConsts& c = a.c;
+    const RainStep& r = a.rain;
+    const int n = c.n;
+    const int tid = threadIdx.x;
+    const int gx0 = tx0 - HX, gy0 = ty0 - 1;
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, X_N * H_BOX * sizeof(float));
+#pragma unroll
+        for (int f = 0; f < X_N; ++f) tma_load_2d(sm + f * H_RC, &a.maps[f], gx0, gy0, bar);
+    }
+    constexpr int RG = (RW / 4) * H_RH;
+    constexpr int RGK = (RG + NTH - 1) / NTH;
+    uint32_t words[RGK][4];
+#pragma unroll
+    for (int k = 0; k < RGK; ++k) {
+        words[k][0] = words[k][1] = words[k][2] = words[k][3] = 0;
+        int q = tid + k * NTH;
+        if (q < RG && r.active && r.bernoulli) {
+            int gx = gx0 + (q % (RW / 4)) * 4, gy = gy0 + q / (RW / 4);
+            if (!EDGE || (gx >= 0 && gx < n && gy >= 0 && gy < n)) rain_words4(r, gx, gy, words[k]);
+        }
+    }
+    // the cell's adjoint inputs, loaded while the tile flies
+    const int ix = tid % TW, iy = tid / TW;
+    const int x = tx0 + ix, y = ty0 + iy;
+    const size_t i = (size_t)y * n + x;
+    float ab, ad, af[4];
+    adj_view_at(a.A, n, x, y, i, ab, ad, af);
+    const float as = a.dse[i];
+    const float DUs = a.du[i], DVs = a.dv[i];
+    const float Ks_i = c.ks_field ? c.ks_field[i] : c.Ks0;
+    bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+        mbar_wait(bar, 0);
+        return;
+    }
+    if (r.active) {
+        float* D = sm + X_D * H_RC;
+#pragma unroll
+        for (int k = 0; k < RGK; ++k) {
+            int q = tid + k * NTH;
+            if (q >= RG) continue;
+            int rx = (q % (RW / 4)) * 4, ry = q / (RW / 4);
+            int gx = gx0 + rx, gy = gy0 + ry;
+            if (EDGE && !(gx >= 0 && gx < n && gy >= 0 && gy < n)) continue;
+            float* p = D + ry * RW + rx;
+            p[0] += rain_incr(r, words[k][0]);
+            p[1] += rain_incr(r, words[k][1]);
+            p[2] += rain_incr(r, words[k][2]);
+            p[3] += rain_incr(r, words[k][3]);
+        }
+    }
+    __syncthreads();
+    const float* B = sm + X_B * H_RC;
+    const float* D = sm + X_D * H_RC;
+    const float* S = sm + X_S * H_RC;
+    const float* F[4] = {sm + X_FL * H_RC, sm + X_FR * H_RC, sm + X_FT * H_RC, sm + X_FB * H_RC};
+    {
+        const int si = (1 + iy) * RW + HX + ix;
+        const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
+        const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
+        // ---- forward recompute: flux --------------------------------------
+        const float b = B[si], d1 = D[si];
+        const float bl = B[si - 1], br = B[si + 1], bb = B[si - RW], bt = B[si + RW];
+        const float f[4] = {F[0][si], F[1][si], F[2][si], F[3][si]};
+        const float wn[4] = {has_l ? bl + D[si - 1] : FAR_HEIGHT, has_r ? br + D[si + 1] : FAR_HEIGHT,
+                             has_t ? bt + D[si + RW] : FAR_HEIGHT, has_b ? bb + D[si - RW] : FAR_HEIGHT};
+        const float in[4] = {has_l ? F[1][si - 1] : 0.0f, has_r ? F[0][si + 1] : 0.0f,
+                             has_t ? F[3][si + RW] : 0.0f, has_b ? F[2][si - RW] : 0.0f};
+        const FluxFwd fw = flux_fwd(c, x, y, b + d1, d1, f, wn, in, EDGE);
+        // ---- forward recompute: erosion speed and tilt ---------------------
+        const float u = fw.u, v = fw.v, vz = fw.vz;
+        const float len = sqrtf(u * u + v * v);
+        float ero = len, dero_dlen = 1.0f, dero_dvz = 0.0f;
+        if (vz < 1e-3f) {
+            float dd = gmax(5e-4f, vz);
+            float tr = (dd - 1e-3f) / (5e-4f - 1e-3f);
+            float t = gclamp(tr, 0.0f, 1.0f);
+            float sm3 = t * t * (3.0f - 2.0f * t);
+            ero = gmix(len, 0.0f, sm3);
+            dero_dlen = 1.0f - sm3;
+            // d(smoothstep)/d(vz): 6 t (1 - t) / (5e-4 - 1e-3)
+            if (vz > 5e-4f && tr > 0.0f && tr < 1.0f) dero_dvz = len * 6.0f * t * (1.0f - t) * 2000.0f;
+        }
+        const float ebr = has_r ? br : 0.0f, ebl = has_l ? bl : 0.0f;
+        const float ebt = has_t ? bt : 0.0f, ebb = has_b ? bb : 0.0f;
+        const float dx = ebr - ebl, dz = ebt - ebb;
+        const float cx = dx * 2.0f - 0.0f * dz, cz = 2.0f * dz - dx * 0.0f;
+        const float L3 = sqrtf(cx * cx + 16.0f + cz * cz);
+        const float ny = -4.0f / L3;
+        const float sin_a = fabsf(sqrtf(1.0f - ny * ny));
+        const float sa = gmax(0.02f, sin_a);
+        const float craw = c.Kc * sa * ero;
+        const float cc = gmax(0.0f, craw);
+        const float Kls = c.dt * Ks_i, Kld = c.Kld0, s = S[si];
+        // ---- erosion reversed ----------------------------------------------
+        a.dse[i] = 0.0f;  // free for the step after next
+        float gb, gs, gc = 0.0f, gKs = 0.0f;
+        if (cc > 0.0f && !(c.Kls1 * cc > 0.0f)) {  // the empty dirt layer ends the layer loop: identity
+            gb = ab;
+            gs = as;
+        } else if (cc > s) {
+            float del = Kls * (cc - s);
+            if (b - del < 0.0f) {  // rock exhausted: b' = 0, s' = s + b
+                gb = as;
+                gs = as;
+            } else {
+                gb = ab;
+                gs = ab * Kls + as * (1.0f - Kls);
+                gc = (as - ab) * Kls;
+                gKs = (as - ab) * (cc - s);
+            }
+        } else {
+            gb = ab;
+            gs = ab * Kld + as * (1.0f - Kld);
+            gc = (as - ab) * Kld;
+        }
+        if (gKs != 0.0f) a.dks[i] += gKs * c.dt;
+        float pdx = 0.0f, pdz = 0.0f, due = 0.0f, dve = 0.0f, gvz = 0.0f;
+        if (craw > 0.0f) {
+            float gsa = gc * c.Kc * ero, gero = gc * c.Kc * sa;
+            if (sin_a > 0.02f) {
+                const float r3 = __frcp_rn(L3);
+                float gny = gsa * (-ny * __frcp_rn(sin_a));
+                float gL3 = gny * (4.0f * r3 * r3);
+                pdx = gL3 * 4.0f * dx * r3;
+                pdz = gL3 * 4.0f * dz * r3;
+            }
+            float glen = gero * dero_dlen;
+            gvz = gero * dero_dvz;
+            if (len > 0.0f) {
+                const float rl = __frcp_rn(len);
+                due = glen * u * rl;
+                dve = glen * v * rl;
+            }
+        }
+        // ---- flux reversed -------------------------------------------------
+        const float DU = DUs + due, DV = DVs + dve;
+        float gin[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gfown[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (vz > 0.0f) {
+            const float rv = __frcp_rn(vz);
+            float gu = DU * rv, gv = DV * rv;
+            gin[0] += gu; gin[1] -= gu;
+            gfown[0] -= gu; gfown[1] += gu;
+            gin[3] += gv; gin[2] -= gv;
+            gfown[3] -= gv; gfown[2] += gv;
+            gvz -= (DU * u + DV * v) * rv;
+        }
+        float gd1 = gvz, gd2 = gvz + ad * c.evap;
+        float garg = fw.arg > 0.0f ? gd2 : 0.0f;
+        gd1 += garg;
+        float gsum_in = c.dt * garg, gsum_outK = -c.dt * garg;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) gin[d] += gsum_in;
+        float gK = gsum_outK * fw.sum_out, gsum_out = gsum_outK * fw.K;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) gK += af[d] * fw.g[d];
+        float gg[4];
+#pragma unroll
+        for (int d = 0; d < 4; ++d) gg[d] = af[d] * fw.K + gsum_out;
+        if (fw.scaled) {
+            const float rd = __frcp_rn(fw.den);
+            gd1 += gK * rd;
+            float gden = -gK * d1 * rd * rd;
+#pragma unroll
+            for (int d = 0; d < 4; ++d) gg[d] += gden * c.dt;
+        }
+        float gw = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            float gdh = 0.0f;
+            if (fw.live[d]) {
+                gfown[d] += c.EK * gg[d];
+                gdh = c.dt * c.G * gg[d];
+                gw += gdh;
+            }
+            a.pdh[d][i] = gdh;
+            a.pin[d][i] = gin[d];
+            a.rf[d][i] = gfown[d];
+        }
+        a.pdx[i] = pdx;
+        a.pdz[i] = pdz;
+        a.rb[i] = gb + gw;
+        a.rd[i] = gw + gd1;
+        a.rs[i] = gs;
+        // ---- sediment_transport of step j - 1 reversed ----------------------
+        if (a.scatter_prev) sediment_adjoint(c, a.prev, x, y, i, gs, a.dse_prev, a.du, a.dv);
+    }
+}
+
+__global__ void __launch_bounds__(NTH) k_adj_cell(const __grid_constant__ AdjCellArgs a, int* err) {
+    __shared__ __align__(128) float sm[X_N * H_RC];
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    const int n = a.c.n;
+    const int tiles_x = n / TW;
+    const int tx0 = (blockIdx.x % tiles_x) * TW, ty0 = (blockIdx.x / tiles_x) * TH;
+    bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 1 >= 0 && ty0 + TH + 1 <= n;
+    if (inner) adj_tile<false>(a, sm, &bar, tx0, ty0, err);
+    else adj_tile<true>(a, sm, &bar, tx0, ty0, err);
+}
+
+// ---- k_adj_final -----------------------------------------------------------------
+__global__ void k_adj_final(int n, AdjView A, float* __restrict__ out_b) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= n || y >= n) return;
+    size_t i = at(n, x, y);
+    float ab, ad, af[4];
+    adj_view_at(A, n, x, y, i, ab, ad, af);
+    out_b[i] = ab;
 }
 
 // d(mean((rock - target)^2))/d rock, and the loss partials
@@ -310,18 +403,25 @@ dim3 grid_for(int n) { return dim3((n + BX - 1) / BX, (n + BY - 1) / BY); }
 
 }  // namespace
 
-void launch_adjoint_step(const StepConsts& c, const RainStep& r, const AdjFields& X, const AdjFields& A,
-                         const AdjFields& R, const AdjTemps& T, const AdjWork& W, float* dks, cudaStream_t st) {
-    const int n = c.n;
-    dim3 blk(BX, BY), g = grid_for(n), g4((n / 4 + BX - 1) / BX, (n + BY - 1) / BY);
-    k_adj_rain<<<g4, blk, 0, st>>>(c, r, X.d, T.dr);
-    k_adj_recompute<<<g, blk, 0, st>>>(c, X, T);
-    cudaMemsetAsync(W.dse, 0, (size_t)n * n * sizeof(float), st);
-    k_adj_sediment<<<g, blk, 0, st>>>(c, A, T, W);
-    k_adj_erosion<<<g, blk, 0, st>>>(c, X, A, T, W, dks);
-    k_adj_flux<<<g, blk, 0, st>>>(c, X, A, T, W);
-    k_adj_gather<<<g, blk, 0, st>>>(n, W, R);
-    count_launch(6);
+bool adjoint_tile_ok(int n) { return n % TW == 0 && n % TH == 0; }
+
+int adjoint_box_rows() { return H_RH; }
+
+void launch_adjoint_sediment(const StepConsts& c, const AdjSlot& slot, const float* as, float* dse, float* du,
+                             float* dv, cudaStream_t st) {
+    k_adj_sediment<<<grid_for(c.n), dim3(BX, BY), 0, st>>>(c, slot, as, dse, du, dv);
+    count_launch();
+}
+
+void launch_adjoint_cell(const AdjCellArgs& args, int* err, cudaStream_t st) {
+    const int n = args.c.n;
+    k_adj_cell<<<(n / TW) * (n / TH), NTH, 0, st>>>(args, err);
+    count_launch();
+}
+
+void launch_adjoint_final(int n, const AdjView& A, float* out_b, cudaStream_t st) {
+    k_adj_final<<<grid_for(n), dim3(BX, BY), 0, st>>>(n, A, out_b);
+    count_launch();
 }
 
 void launch_mse(const float* b, const float* target, size_t count, float* grad, double* part, int nparts,

@@ -119,22 +119,58 @@ struct AdjFields {
     float* s;
     float* f[4];
 };
-// Forward intermediates recomputed for the reversed step.
-struct AdjTemps {
-    float *dr, *u, *v, *vz, *d2, *be, *se;
+// Forward intermediates of one step kept by the segment recompute.
+struct AdjSlot {
+    const float* u;
+    const float* v;
+    const float* se;  // eroded sediment
 };
-// Adjoint work fields: per-cell terms and neighbour packets.
-struct AdjWork {
-    float *dse, *du, *dv, *dvz, *dd2, *rb, *rs, *pdx, *pdz, *wbar, *gd1;
-    float* pdh[4];
+// packet fields of a state adjoint: height-difference terms toward L, R, T,
+// B, inflow terms from L, R, T, B, terrain-normal x and z terms
+constexpr int ADJ_PACKET_FIELDS = 10;
+// Adjoint of a state: each cell's own terms (rock, water, fluxes) plus the
+// packets of the terms of its neighbours' inputs; the sediment adjoint needs
+// no packets.
+struct AdjView {
+    const float* b;
+    const float* d;
+    const float* f[4];
+    const float* pdh[4];
+    const float* pin[4];
+    const float* pdx;
+    const float* pdz;
+};
+// Arguments of k_adj_cell (one kernel parameter).
+struct AdjCellArgs {
+    CUtensorMap maps[7];  // X: rock, water, sediment, fL, fR, fT, fB (64-wide tiles, 1-cell halo)
+    StepConsts c;
+    RainStep rain;
+    AdjView A;            // adjoint of the step's output
+    float* dse;           // this step's sediment adjoint (read, then cleared)
+    float* dse_prev;      // step j - 1's sediment adjoint (scatter target)
+    float* du;            // back-trace velocity adjoint: read for step j, written for step j - 1
+    float* dv;
+    AdjSlot prev;         // step j - 1's intermediates
+    int scatter_prev;     // reverse step j - 1's sediment pass here (its intermediates exist)
+    float* rb;            // R: own terms of the input adjoint
+    float* rd;
+    float* rs;
+    float* rf[4];
+    float* pdh[4];        // R: packets
     float* pin[4];
-    float* fown[4];
+    float* pdx;
+    float* pdz;
+    float* dks;           // per-cell Ks gradient (accumulated)
 };
-constexpr int ADJ_WORK_FIELDS = 23;
-// Reverses one step: A (adjoint of the step's outputs) -> R (adjoint of its
-// inputs X); accumulates the per-cell Ks gradient into dks.
-void launch_adjoint_step(const StepConsts& c, const RainStep& r, const AdjFields& X, const AdjFields& A,
-                         const AdjFields& R, const AdjTemps& T, const AdjWork& W, float* dks, cudaStream_t st);
+bool adjoint_tile_ok(int n);
+// Rows of the TMA box k_adj_cell stages per field (tile rows plus halo);
+// AdjCellArgs::maps must be encoded with this box height.
+int adjoint_box_rows();
+void launch_adjoint_sediment(const StepConsts& c, const AdjSlot& slot, const float* as, float* dse, float* du,
+                             float* dv, cudaStream_t st);
+void launch_adjoint_cell(const AdjCellArgs& args, int* err, cudaStream_t st);
+// gathered rock adjoint of a state into out_b
+void launch_adjoint_final(int n, const AdjView& A, float* out_b, cudaStream_t st);
 // loss = mean((b - target)^2) into *out (device), grad = dloss/db (optional).
 void launch_mse(const float* b, const float* target, size_t count, float* grad, double* part, int nparts,
                 double* out, cudaStream_t st);

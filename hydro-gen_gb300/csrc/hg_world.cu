@@ -1026,20 +1026,26 @@ int hg_sync(hg_world* w) {
 
 struct hg_tape {
     hg_world* w = nullptr;
-    hg_world* shadow = nullptr;  // recomputes segments from checkpoints
     int nsteps = 0, K = 0, nseg = 0;
     uint64_t step0 = 0;
     bool recorded = false;
-    float* ckpt = nullptr;  // nseg states (segment starts)
-    float* seg = nullptr;   // K states (inputs of a segment's steps)
-    float* adj = nullptr;   // 2 adjoint states
-    float* temps = nullptr; // 7 recomputed fields
-    float* work = nullptr;  // ADJ_WORK_FIELDS fields
-    float* dks = nullptr;   // per-cell Ks gradient
+    bool last_ready = false;  // the last segment's states and intermediates are in seg / slots
+    float* ckpt = nullptr;   // nseg states: the input of each segment's first step
+    float* seg = nullptr;    // K states: slot j >= 1 the input of a segment's step j,
+                             // slot 0 receives the (unused) output of its last step
+    float* slots = nullptr;  // K x (u, v, eroded sediment) of a segment's steps
+    float* adj = nullptr;    // 2 adjoint states (own terms), alternating A / R
+    float* pk = nullptr;     // their 2 x ADJ_PACKET_FIELDS neighbour packets
+    float* aux = nullptr;    // 2 sediment-adjoint buffers, du, dv, eroded-rock scratch
+    float* dks = nullptr;    // per-cell Ks gradient
+    unsigned long long* d_step = nullptr;  // step counter of the recompute launches
+    TmaCache tma;
 };
 
 namespace {
 constexpr int kStateFields = 7;
+constexpr int kSlotFields = 3;
+constexpr int kAuxFields = 5;
 
 AdjFields fields_at(float* base, size_t c) {
     AdjFields f;
@@ -1051,9 +1057,8 @@ AdjFields fields_at(float* base, size_t c) {
 }
 
 void free_tape(hg_tape* t) {
-    cudaFree(t->ckpt); cudaFree(t->seg); cudaFree(t->adj); cudaFree(t->temps); cudaFree(t->work);
-    cudaFree(t->dks);
-    if (t->shadow) hg_world_destroy(t->shadow);
+    cudaFree(t->ckpt); cudaFree(t->seg); cudaFree(t->slots); cudaFree(t->adj); cudaFree(t->pk);
+    cudaFree(t->aux); cudaFree(t->dks); cudaFree(t->d_step);
 }
 
 // state fields of a world (current buffers) -> contiguous state at dst
@@ -1064,11 +1069,10 @@ int copy_state_out(hg_world* w, float* dst, cudaStream_t st) {
     return HG_OK;
 }
 
-int copy_state_in(hg_world* w, const float* src, cudaStream_t st) {
-    size_t c = cells(w);
-    for (int f = 0; f < kStateFields; ++f)
-        HG_CUDA(cudaMemcpyAsync(w->cur[f], src + f * c, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    return HG_OK;
+size_t tape_bytes(size_t c, int nsteps, int K) {
+    const size_t nseg = (size_t)(nsteps + K - 1) / K;
+    return ((nseg + K) * kStateFields + (size_t)K * kSlotFields + 2 * kStateFields + 2 * ADJ_PACKET_FIELDS +
+            kAuxFields + 1) * c * sizeof(float);
 }
 }  // namespace
 
@@ -1078,18 +1082,18 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     *out = nullptr;
     if (nsteps < 1) return fail(HG_ERR_INVALID, "nsteps must be >= 1");
     if (thermal_on(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion");
-    if (!fused_tile_ok(w->n, 16)) return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
+    if (!fused_tile_ok(w->n, 16) || !adjoint_tile_ok(w->n))
+        return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
     DeviceGuard g(w->device);
-    const size_t c = cells(w), state_bytes = kStateFields * c * sizeof(float);
+    const size_t c = cells(w);
     int K = ckpt_every;
     if (K == HG_AUTO || K <= 0) {
-        // memory holds nsteps/K checkpoints plus K segment states: ~sqrt(nsteps)
+        // checkpoints (nsteps/K states) plus segment buffers (K states and
+        // slots): ~sqrt(nsteps), fewer when half the free memory cannot hold it
         K = (int)std::ceil(std::sqrt((double)nsteps));
         size_t free_b = 0, total_b = 0;
-        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-            size_t fit = free_b / 2 / state_bytes;  // keep half of the free memory
-            while (K > 1 && (size_t)(K + (nsteps + K - 1) / K) > fit) --K;
-        }
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+            while (K > 1 && tape_bytes(c, nsteps, K) > free_b / 2) --K;
     }
     K = std::min(K, nsteps);
     hg_tape* t = new (std::nothrow) hg_tape();
@@ -1098,24 +1102,21 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     t->nsteps = nsteps;
     t->K = K;
     t->nseg = (nsteps + K - 1) / K;
-    cudaError_t e = cudaMalloc((void**)&t->ckpt, t->nseg * state_bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&t->seg, (size_t)K * state_bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&t->adj, 2 * state_bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&t->temps, state_bytes);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&t->work, ADJ_WORK_FIELDS * c * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&t->dks, c * sizeof(float));
+    const size_t fb = c * sizeof(float);
+    cudaError_t e = cudaMalloc((void**)&t->ckpt, (size_t)t->nseg * kStateFields * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->seg, (size_t)K * kStateFields * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->slots, (size_t)K * kSlotFields * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->adj, 2 * kStateFields * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->pk, 2 * ADJ_PACKET_FIELDS * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->aux, kAuxFields * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->dks, fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->d_step, sizeof(unsigned long long));
     if (e != cudaSuccess) {
         free_tape(t);
         delete t;
         int code = e == cudaErrorMemoryAllocation ? HG_ERR_OOM : HG_ERR_CUDA;
         cudaGetLastError();
         return fail(code, std::string("tape allocation: ") + cudaGetErrorString(e));
-    }
-    int rc = hg_world_create(w->n, w->layers, &t->shadow);
-    if (rc != HG_OK) {
-        free_tape(t);
-        delete t;
-        return rc;
     }
     *out = t;
     return HG_OK;
@@ -1137,6 +1138,39 @@ int hg_tape_info(const hg_tape* t, int* nsteps, int* ckpt_every) {
     return HG_OK;
 }
 
+// Recomputes segment s from its checkpoint with the fused step: step j reads
+// its input state (checkpoint or seg slot j) and writes the next state into
+// seg slot j + 1 and u, v, eroded sediment into its slots; the last step's
+// state goes to `last_out` (7 fields) or seg slot 0.  No state copies.
+int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th, float* const* last_out) {
+    hg_world* w = t->w;
+    const size_t c = cells(w), sf = kStateFields * c;
+    k_set_u64<<<1, 1, 0, w->stream>>>(t->d_step, (unsigned long long)(t->step0 + (uint64_t)s * t->K));
+    TerrainSrc src{};
+    src.c = cst;
+    src.rain = make_rain_base(w);
+    src.b_ero = t->aux + 4 * c;
+    src.step = t->d_step;
+    TerrainDesc td;
+    for (int j = 0; j < len; ++j) {
+        const float* in = j == 0 ? t->ckpt + (size_t)s * sf : t->seg + (size_t)j * sf;
+        float* outp = t->seg + (size_t)(j + 1 < len ? j + 1 : 0) * sf;
+        for (int f = 0; f < S_COUNT; ++f) {
+            src.in[f] = in + f * c;
+            src.out[f] = (j + 1 == len && last_out) ? last_out[f] : outp + f * c;
+        }
+        float* sl = t->slots + (size_t)j * kSlotFields * c;
+        src.u = sl;
+        src.v = sl + c;
+        src.s_ero = sl + 2 * c;
+        if (!fill_desc(td, src, th, 0, t->tma))
+            return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
+        launch_fused_one(td, th, w->err, w->stream);
+    }
+    HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+
 int hg_forward(hg_tape* t) {
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     hg_world* w = t->w;
@@ -1147,10 +1181,26 @@ int hg_forward(hg_tape* t) {
     for (int s = 0; s < t->nseg; ++s) {
         int rc = copy_state_out(w, t->ckpt + (size_t)s * kStateFields * c, w->stream);
         if (rc != HG_OK) return rc;
-        rc = hg_step(w, std::min(t->K, t->nsteps - s * t->K), HG_MODE_FUSED);
+        const int len = std::min(t->K, t->nsteps - s * t->K);
+        if (s + 1 < t->nseg) {
+            rc = hg_step(w, len, HG_MODE_FUSED);
+            if (rc != HG_OK) return rc;
+            continue;
+        }
+        // the last segment steps through the tape's buffers: its states and
+        // intermediates stay for the backward sweep, the final state lands in
+        // the world's alternate buffers
+        rc = recompute_segment(t, s, len, make_consts(w), w->tuning.th ? w->tuning.th : 16, w->alt);
         if (rc != HG_OK) return rc;
+        for (int f = 0; f < S_COUNT; ++f) std::swap(w->cur[f], w->alt[f]);
+        w->step += (uint64_t)len;
+        w->dev_step_valid = false;
+        const float* sl = t->slots + (size_t)(len - 1) * kSlotFields * c;
+        HG_CUDA(cudaMemcpyAsync(w->u, sl, c * sizeof(float), cudaMemcpyDeviceToDevice, w->stream));
+        HG_CUDA(cudaMemcpyAsync(w->v, sl + c, c * sizeof(float), cudaMemcpyDeviceToDevice, w->stream));
     }
     t->recorded = true;
+    t->last_ready = true;
     return HG_OK;
 }
 
@@ -1159,66 +1209,85 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
     if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
     hg_world* w = t->w;
-    hg_world* sh = t->shadow;
+    if (thermal_on(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion");
     DeviceGuard g(w->device);
     cudaStream_t st = w->stream;
     const size_t c = cells(w), sf = kStateFields * c;
-    // the shadow world recomputes segments with the world's settings
-    sh->es = w->es;
-    sh->rs = w->rs;
-    sh->opt = w->opt;
-    sh->version += 1;
-    if (w->ks_on) HG_CUDA(cudaMemcpyAsync(sh->ks, w->ks, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    sh->ks_on = w->ks_on;
     const StepConsts cst = make_consts(w);
-    AdjFields A = fields_at(t->adj, c), R = fields_at(t->adj + sf, c);
-    AdjTemps T;
-    float* tp = t->temps;
-    T.dr = tp; T.u = tp + c; T.v = tp + 2 * c; T.vz = tp + 3 * c; T.d2 = tp + 4 * c; T.be = tp + 5 * c;
-    T.se = tp + 6 * c;
-    AdjWork W;
-    float* wp = t->work;
-    float** named[] = {&W.dse, &W.du, &W.dv, &W.dvz, &W.dd2, &W.rb, &W.rs, &W.pdx, &W.pdz, &W.wbar, &W.gd1};
-    int k = 0;
-    for (float** p : named) *p = wp + (size_t)(k++) * c;
-    for (int d = 0; d < 4; ++d) {
-        W.pdh[d] = wp + (size_t)(k++) * c;
-        W.pin[d] = wp + (size_t)(k++) * c;
-        W.fown[d] = wp + (size_t)(k++) * c;
-    }
+    const int th = w->tuning.th ? w->tuning.th : 16;
+    // state adjoints alternate between two buffers of own terms and packets
+    AdjFields own[2] = {fields_at(t->adj, c), fields_at(t->adj + sf, c)};
+    float* pkb[2] = {t->pk, t->pk + ADJ_PACKET_FIELDS * c};
+    auto view = [&](int k) {
+        AdjView v;
+        v.b = own[k].b;
+        v.d = own[k].d;
+        for (int d = 0; d < 4; ++d) {
+            v.f[d] = own[k].f[d];
+            v.pdh[d] = pkb[k] + (size_t)d * c;
+            v.pin[d] = pkb[k] + (size_t)(4 + d) * c;
+        }
+        v.pdx = pkb[k] + 8 * c;
+        v.pdz = pkb[k] + 9 * c;
+        return v;
+    };
+    float* dse[2] = {t->aux, t->aux + c};
+    float* du = t->aux + 2 * c;
+    float* dv = t->aux + 3 * c;
+    // the final state's adjoint: rock only, no packets
     HG_CUDA(cudaMemsetAsync(t->adj, 0, 2 * sf * sizeof(float), st));
-    HG_CUDA(cudaMemcpyAsync(A.b, dL_drock_final, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    HG_CUDA(cudaMemsetAsync(t->pk, 0, 2 * ADJ_PACKET_FIELDS * c * sizeof(float), st));
+    HG_CUDA(cudaMemsetAsync(t->aux, 0, 2 * c * sizeof(float), st));  // scatter targets start at zero
+    HG_CUDA(cudaMemcpyAsync(own[0].b, dL_drock_final, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
     HG_CUDA(cudaMemsetAsync(t->dks, 0, c * sizeof(float), st));
-    cudaEvent_t ev;
-    HG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    int rc = HG_OK;
-    for (int s = t->nseg - 1; s >= 0 && rc == HG_OK; --s) {
+    auto slot_of = [&](int j) {
+        const float* sl = t->slots + (size_t)j * kSlotFields * c;
+        return AdjSlot{sl, sl + c, sl + 2 * c};
+    };
+    AdjCellArgs args;
+    args.c = cst;
+    args.du = du;
+    args.dv = dv;
+    args.dks = t->dks;
+    int cur = 0;      // buffer holding the adjoint of the next reversed step's output
+    uint64_t m = 0;   // reversed steps so far: step m uses dse[m & 1]
+    for (int s = t->nseg - 1; s >= 0; --s) {
         const int len = std::min(t->K, t->nsteps - s * t->K);
-        const float* ck = t->ckpt + (size_t)s * sf;
-        HG_CUDA(cudaMemcpyAsync(t->seg, ck, sf * sizeof(float), cudaMemcpyDeviceToDevice, st));
-        if (len > 1) {  // inputs of the segment's later steps, recomputed on the shadow world
-            if ((rc = copy_state_in(sh, ck, st)) != HG_OK) break;
-            HG_CUDA(cudaEventRecord(ev, st));
-            HG_CUDA(cudaStreamWaitEvent(sh->stream, ev, 0));
-            sh->step = t->step0 + (uint64_t)s * t->K;
-            sh->dev_step_valid = false;
-            for (int j = 1; j < len && rc == HG_OK; ++j) {
-                rc = hg_step(sh, 1, HG_MODE_FUSED);
-                if (rc == HG_OK) rc = copy_state_out(sh, t->seg + (size_t)j * sf, sh->stream);
-            }
-            HG_CUDA(cudaEventRecord(ev, sh->stream));
-            HG_CUDA(cudaStreamWaitEvent(st, ev, 0));
+        if (!(s + 1 == t->nseg && t->last_ready)) {  // the forward left the last segment in place
+            int rc = recompute_segment(t, s, len, cst, th, nullptr);
+            if (rc != HG_OK) return rc;
         }
-        for (int j = len - 1; j >= 0 && rc == HG_OK; --j) {
-            AdjFields X = fields_at(t->seg + (size_t)j * sf, c);
-            RainStep r = make_rain(w, t->step0 + (uint64_t)s * t->K + j + 1);
-            launch_adjoint_step(cst, r, X, A, R, T, W, t->dks, st);
-            std::swap(A, R);
+        // the segment's last step: its sediment pass reversed on its own
+        launch_adjoint_sediment(cst, slot_of(len - 1), own[cur].s, dse[m & 1], du, dv, st);
+        for (int j = len - 1; j >= 0; --j, ++m) {
+            const float* xin = j == 0 ? t->ckpt + (size_t)s * sf : t->seg + (size_t)j * sf;
+            for (int f = 0; f < kStateFields; ++f)
+                if (!t->tma.get(xin + f * c, w->n, adjoint_box_rows(), &args.maps[f]))
+                    return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
+            args.rain = make_rain(w, t->step0 + (uint64_t)s * t->K + j + 1);
+            args.A = view(cur);
+            args.dse = dse[m & 1];
+            args.dse_prev = dse[(m + 1) & 1];
+            args.scatter_prev = j > 0 ? 1 : 0;
+            args.prev = j > 0 ? slot_of(j - 1) : AdjSlot{nullptr, nullptr, nullptr};
+            const AdjFields& R = own[cur ^ 1];
+            args.rb = R.b;
+            args.rd = R.d;
+            args.rs = R.s;
+            AdjView rv = view(cur ^ 1);
+            for (int d = 0; d < 4; ++d) {
+                args.rf[d] = R.f[d];
+                args.pdh[d] = const_cast<float*>(rv.pdh[d]);
+                args.pin[d] = const_cast<float*>(rv.pin[d]);
+            }
+            args.pdx = const_cast<float*>(rv.pdx);
+            args.pdz = const_cast<float*>(rv.pdz);
+            launch_adjoint_cell(args, w->err, st);
+            cur ^= 1;
         }
     }
-    cudaEventDestroy(ev);
-    if (rc != HG_OK) return rc;
-    if (dL_drock0) HG_CUDA(cudaMemcpyAsync(dL_drock0, A.b, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    if (t->nseg > 1) t->last_ready = false;  // other segments' recomputes reused the buffers
+    if (dL_drock0) launch_adjoint_final(w->n, view(cur), dL_drock0, st);
     if (dL_dks) HG_CUDA(cudaMemcpyAsync(dL_dks, t->dks, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
     HG_CUDA(cudaGetLastError());
     return HG_OK;
