@@ -129,6 +129,7 @@ struct StepConsts {
     float talus_x_cross;  // smallest positive slope whose poly_atanf exceeds Kalpha0
     float talus_b_diag;   // smallest positive height drop whose diagonal slope does
     int fast_div;         // both thresholds >= 2^-30: outflow quotients by div_recip
+    float smooth_m;       // smoothing weight clamp(Kspeed[1]*d_t, 0, 1); 0: the pass is the identity
 };
 
 // ---- hydro_flux, glsl/hydro_flux.glsl:77-166 -------------------------------------
@@ -355,6 +356,22 @@ __device__ __forceinline__ float cell_thermal_apply(float b, const float own[8],
     for (int k = 0; k < 8; ++k) sum -= own[k];
     sum += in_flux;
     return b + sum;
+}
+
+// ---- smoothing, glsl/smoothing.glsl:22-103 (grid branch), rock channel -----------
+// Interior cell with rock tr and neighbours lr, rr, tt (y+1), bt (y-1); border
+// cells are copied by the caller.  With the dirt channel at 0 the dirt
+// differences equal the rock differences (0 - 0 + d == d) and the dirt average
+// is 0, so dirt stays exactly 0 and only rock changes: a local extremum along
+// x or y moves toward its 4-neighbour mean by the weight m.
+__device__ __forceinline__ float cell_smooth(float m, float tr, float lr, float rr, float tt, float bt) {
+    float dl = tr - lr, dr = tr - rr, dt_ = tr - tt, db = tr - bt;
+    float hdiff = fabsf((dl + dr + dt_ + db) / 4.0f);
+    float xs = dl * dr, ys = dt_ * db;
+    float nr = tr;
+    if (((-dl > hdiff || -dr > hdiff) && xs > 0.0f) || ((-dt_ > hdiff || -db > hdiff) && ys > 0.0f))
+        nr = (tr + lr + rr + tt + bt) / 5.0f;
+    return m * nr + (1.0f - m) * tr;
 }
 
 }  // namespace hg

@@ -34,6 +34,8 @@ void launch_sediment(const StepConsts& c, const float* u, const float* v, const 
 void launch_thermal_out(const StepConsts& c, const float* rock, float4* tc, float4* td, cudaStream_t st);
 void launch_thermal_in(const StepConsts& c, const float* rock, const float4* tc, const float4* td,
                        float* rock_o, cudaStream_t st);
+// smoothing pass on rock (run when c.smooth_m != 0)
+void launch_smooth(const StepConsts& c, const float* rock, float* rock_o, cudaStream_t st);
 
 // ---- fused step (hg_fused.cu) ---------------------------------------------------
 // Rain settings without the step number (the kernels add the step).

@@ -146,6 +146,20 @@ __global__ void k_thermal_in(StepConsts c, const float* __restrict__ rock, const
     rock_o[i] = cell_thermal_apply(rock[i], own, in);
 }
 
+// glsl/smoothing.glsl:22-103, rock channel (see cell_smooth)
+__global__ void k_smooth(StepConsts c, const float* __restrict__ rock, float* __restrict__ rock_o) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int n = c.n;
+    if (x >= n || y >= n) return;
+    size_t i = at(n, x, y);
+    if (x == 0 || y == 0 || x == n - 1 || y == n - 1) {  // border texels are copied (:27-33)
+        rock_o[i] = rock[i];
+        return;
+    }
+    rock_o[i] = cell_smooth(c.smooth_m, rock[i], rock[i - 1], rock[i + 1], rock[i + n], rock[i - n]);
+}
+
 dim3 grid_for(int n) { return dim3((n + BX - 1) / BX, (n + BY - 1) / BY); }
 
 }  // namespace
@@ -184,6 +198,11 @@ void launch_thermal_out(const StepConsts& c, const float* rock, float4* tc, floa
 void launch_thermal_in(const StepConsts& c, const float* rock, const float4* tc, const float4* td,
                        float* rock_o, cudaStream_t st) {
     k_thermal_in<<<grid_for(c.n), dim3(BX, BY), 0, st>>>(c, rock, tc, td, rock_o);
+    count_launch();
+}
+
+void launch_smooth(const StepConsts& c, const float* rock, float* rock_o, cudaStream_t st) {
+    k_smooth<<<grid_for(c.n), dim3(BX, BY), 0, st>>>(c, rock, rock_o);
     count_launch();
 }
 

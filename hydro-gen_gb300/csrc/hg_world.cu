@@ -124,6 +124,7 @@ struct Plan {
     std::vector<std::array<const float*, S_COUNT>> key_cur, key_alt;  // buffers at build time
     std::vector<uint64_t> versions;
     cudaGraphExec_t graph[2] = {};  // two steps starting with table 0 / table 1
+    uint64_t graph_launches = 4;    // kernel launches in one graph
     cudaStream_t stream = nullptr;
     int* err = nullptr;
 };
@@ -239,6 +240,10 @@ bool thermal_on(const hg_world* w) {
     return w->opt.thermal != 0;
 }
 
+StepConsts make_consts(const hg_world* w);
+// the reversed step covers rain, flux, erosion and sediment transport
+bool adjoint_covers(const hg_world* w) { return !thermal_on(w) && make_consts(w).smooth_m == 0.0f; }
+
 StepConsts make_consts(const hg_world* w) {
     StepConsts c{};
     const hg_erosion_settings& s = w->es;
@@ -267,6 +272,10 @@ StepConsts make_consts(const hg_world* w) {
     if (c.talus_x_cross < tiny) c.talus_x_cross = tiny;
     if (c.talus_b_diag < tiny) c.talus_b_diag = tiny;
     c.fast_div = !(c.talus_x_cross < 0x1p-30f) && !(c.talus_b_diag < 0x1p-30f);
+    // smoothing weight, glsl/smoothing.glsl:74 (GLSL clamp: min(max(x, 0), 1))
+    volatile float k1dt = s.Kspeed[1] * dt;
+    float m = k1dt < 0.0f ? 0.0f : (float)k1dt;
+    c.smooth_m = 1.0f < m ? 1.0f : m;
     return c;
 }
 
@@ -394,6 +403,17 @@ int plan_dir(const Plan* p) {
 void launch_dir(Plan* p, int dir) {
     if (p->worlds.size() == 1) launch_fused_one(p->h_tab[dir][0], p->th, p->err, p->stream);
     else launch_fused_table(*p->bp[dir], p->d_maps[dir], p->total, p->th, p->err, p->stream);
+    // smoothing (worlds with Kspeed[1] != 0): the fused step's rock through
+    // the per-pass smoothing kernel into scratch (the per-pass thermal
+    // buffer) and back
+    for (size_t i = 0; i < p->worlds.size(); ++i) {
+        const TerrainHot& h = p->h_tab[dir][i].h;
+        if (h.c.smooth_m == 0.0f) continue;
+        hg_world* w = p->worlds[i];
+        float* scratch = reinterpret_cast<float*>(w->tc);
+        launch_smooth(h.c, h.out[S_ROCK], scratch, p->stream);
+        cudaMemcpyAsync(h.out[S_ROCK], scratch, cells(w) * sizeof(float), cudaMemcpyDeviceToDevice, p->stream);
+    }
 }
 
 // Brings a plan up to date (tables, device step counters, the graph that
@@ -414,11 +434,13 @@ int prepare_plan(Plan* p, bool use_graph, int* dir_out) {
     const int nt = (int)p->worlds.size();
     if (use_graph && !p->graph[dir]) {
         cudaGraph_t g = nullptr;
+        const uint64_t before = g_launches.load();
         HG_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
         launch_dir(p, dir);
         launch_dir(p, 1 - dir);
         cudaError_t e = cudaStreamEndCapture(p->stream, &g);
-        g_launches.fetch_sub(4);  // captured, not run
+        p->graph_launches = g_launches.load() - before;  // captured, not run
+        g_launches.fetch_sub(p->graph_launches);
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
         e = cudaGraphInstantiate(&p->graph[dir], g, 0);
         cudaGraphDestroy(g);
@@ -438,7 +460,7 @@ int run_plan(Plan* p, int nsteps, bool use_graph) {
     if (use_graph && nsteps >= 2) {
         for (; k + 2 <= nsteps; k += 2) {
             HG_CUDA(cudaGraphLaunch(p->graph[dir], p->stream));
-            count_launch(4);
+            count_launch(p->graph_launches);
         }
     }
     for (; k < nsteps; ++k)
@@ -657,8 +679,6 @@ int hg_set_erosion_settings(hg_world* w, const hg_erosion_settings* s) {
     if (!(s->d_t > 0.0f) || !std::isfinite(s->d_t)) return fail(HG_ERR_INVALID, "d_t must be positive and finite");
     if (w->layers == 1 && s->Kconv != 0.0f)
         return fail(HG_ERR_INVALID, "Kconv must be 0 in a one-layer world (no dirt layer)");
-    if (w->layers == 1 && s->Kspeed[1] != 0.0f)
-        return fail(HG_ERR_INVALID, "Kspeed[1] must be 0 in a one-layer world (dirt slippage and smoothing)");
     w->es = *s;
     w->version += 1;
     return HG_OK;
@@ -827,6 +847,12 @@ int hg_step(hg_world* w, int nsteps, int mode) {
             if (c.thermal) {
                 launch_thermal_out(c, w->cur[S_ROCK], w->tc, w->td, st);
                 launch_thermal_in(c, w->cur[S_ROCK], w->tc, w->td, w->alt[S_ROCK], st);
+                swap(S_ROCK);
+            }
+            // the dirt layer's talus pass moves nothing (its H is min(0, .) == 0);
+            // smoothing changes rock when Kspeed[1] != 0
+            if (c.smooth_m != 0.0f) {
+                launch_smooth(c, w->cur[S_ROCK], w->alt[S_ROCK], st);
                 swap(S_ROCK);
             }
             w->step += 1;
@@ -1081,7 +1107,7 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     if (!out) return fail(HG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (nsteps < 1) return fail(HG_ERR_INVALID, "nsteps must be >= 1");
-    if (thermal_on(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion and smoothing");
     if (!fused_tile_ok(w->n, 16) || !adjoint_tile_ok(w->n))
         return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
     DeviceGuard g(w->device);
@@ -1174,7 +1200,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
 int hg_forward(hg_tape* t) {
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     hg_world* w = t->w;
-    if (thermal_on(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion and smoothing");
     DeviceGuard g(w->device);
     t->step0 = w->step;
     const size_t c = cells(w);
@@ -1209,7 +1235,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
     if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
     hg_world* w = t->w;
-    if (thermal_on(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion and smoothing");
     DeviceGuard g(w->device);
     cudaStream_t st = w->stream;
     const size_t c = cells(w), sf = kStateFields * c;

@@ -113,9 +113,16 @@ def test_inverse_fit_reduces_loss():
     assert losses[-1] < losses[0]
 
 
-def test_adjoint_rejects_thermal():
+def test_adjoint_rejects_thermal_and_smoothing():
     w = H.World(64)
     H.configure(w, "config2")
+    with pytest.raises(H.HydrogenError) as e:
+        H.Tape(w, 4)
+    assert e.value.code == -5
+    H.configure(w, "config1")
+    s = H.settings_config1()
+    s.Kspeed[1] = 1.0
+    w.set_erosion(s)
     with pytest.raises(H.HydrogenError) as e:
         H.Tape(w, 4)
     assert e.value.code == -5

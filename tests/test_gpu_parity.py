@@ -233,6 +233,22 @@ def test_unsupported_and_invalid_requests():
         w.set_erosion(s)
 
 
+@pytest.mark.parametrize("k1,mode", [(5.0, H.MODE_PLAIN), (5.0, H.MODE_FUSED), (100.0, H.MODE_FUSED)])
+def test_smoothing_bitwise_vs_float_oracle(k1, mode):
+    """Kspeed[1] != 0 in the one-layer world: the dirt layer's talus pass moves
+    nothing and smoothing (glsl/smoothing.glsl) acts on rock; the oracle runs
+    the full two-layer model with both passes."""
+    w, ow, s, o = make_pair(128, "config2", p=0.02)
+    es = H.settings_config2()
+    es.Kspeed[1] = k1
+    w.set_erosion(es)
+    s.Kspeed[1] = k1
+    w.step(30, mode)
+    ow.step(s, o, 30)
+    assert_bitwise(w, ow, ctx=f"Kspeed[1] {k1}")
+    assert not np.any(ow.get("dirt"))
+
+
 def test_minimum_grid():
     w, ow, s, o = make_pair(8, "config1")
     w.step(20, H.MODE_PLAIN)
