@@ -1,16 +1,21 @@
-// FP64 reference adjoint of the single-material grid step without thermal
-// erosion — TEST INFRASTRUCTURE ONLY (checks the GPU adjoint; is itself
-// checked against central finite differences of the oracle's FP64 forward).
+// FP64 reference adjoint of the single-material grid step — TEST
+// INFRASTRUCTURE ONLY (checks the GPU adjoint; is itself checked against
+// central finite differences of the oracle's FP64 forward).
 //
 // Forward model (one step, every field FP64, settings widened from float):
 //   rain:      d_r = d + a                       (glsl/rain.glsl:48-53)
 //   flux:      glsl/hydro_flux.glsl:77-166
 //   erosion:   glsl/hydro_erosion.glsl:23-92 (rock layer; empty dirt layer)
 //   sediment:  glsl/sediment_transport.glsl:66-93, img_interpolation.glsl:3-22
+//   thermal:   glsl/thermal_erosion.glsl:28-109, glsl/thermal_transport.glsl:31-65
+//              (layer 0, when Kspeed[0] != 0; the same double operations as
+//              the oracle's thermal passes, with std::atan)
 // Reverse mode with subgradients: max(0, x) and min(1, q) pass the
 // derivative of the taken argument (ties take the constant side), clamps
 // pass 0 when clamped, dissolve/deposit/exhaustion use the taken branch,
-// floor() is locally constant.  Loss = mean((rock_final - target)^2);
+// floor() is locally constant; the talus marks are locally constant, the
+// largest drop H and the steepest slope pass their derivative to the
+// direction that attains them (the first in direction order).  Loss = mean((rock_final - target)^2);
 // gradients with respect to the per-cell rock solubility Ks and the initial
 // rock heights.
 #include <cmath>
@@ -21,9 +26,13 @@
 namespace {
 
 struct Params {
-    double dt, G, EK, Kc, Kd0, Ke, amount;
+    double dt, G, EK, Kc, Kd0, Ke, amount, Kalpha, Kspeed;
     int period;
 };
+
+// thermal directions L, R, T, B, LT, RT, LB, RB
+const int TOX[8] = {-1, 1, 0, 0, -1, 1, -1, 1};
+const int TOY[8] = {0, 0, 1, -1, 1, 1, -1, -1};
 
 struct State {
     std::vector<double> b, d, s, f[4];  // f: L, R, T, B
@@ -128,6 +137,116 @@ struct Model {
                 Y.d[i] = I.d2[i] * (1 - p.Ke * p.dt);
                 Y.b[i] = I.be[i];
             }
+        if (p.Kspeed != 0.0) thermal(I.be, Y.b);
+    }
+
+    // Talus outflows of cell (x, y) of rock field b (the oracle's
+    // thermal_flux_pass for layer 0, in the same double operations).
+    struct Talus {
+        double dh[8], o[8], bk = 0, Hmax = 0, S = 0, s1 = 1, slope = 0;
+        bool mk[8], sharp_taken = false;
+        int jh = -1, js = -1;
+    };
+    Talus talus(const std::vector<double>& b, int x, int y) const {
+        Talus t;
+        const double FARH = 999999999999.0, bc = b[id(x, y)];
+        for (int k = 0; k < 8; ++k) {
+            int xx = x + TOX[k], yy = y + TOY[k];
+            t.dh[k] = 0.0 + (bc - (in(xx, yy) ? b[id(xx, yy)] : FARH));
+        }
+        for (int k = 0; k < 8; ++k)
+            if (t.dh[k] > t.Hmax) { t.Hmax = t.dh[k]; t.jh = k; }
+        double Hh = gmin(bc, t.Hmax);
+        double best_alph = -1e300;
+        for (int k = 0; k < 8; ++k) {
+            t.mk[k] = false;
+            double bb = t.dh[k];
+            if (bb <= 0) continue;
+            double d = 1.0;
+            if (k >= 4) d *= std::sqrt(2.0);
+            double alph = std::atan(bb / d);
+            if (alph > p.Kalpha) {
+                double newsh = 1.0 + alph - p.Kalpha;
+                if (newsh > t.s1) { t.s1 = newsh; t.sharp_taken = true; }
+                if (alph > best_alph) { best_alph = alph; t.js = k; t.slope = bb / d; }
+                t.bk += bb;
+                t.mk[k] = true;
+            }
+        }
+        double sh = t.s1;
+        sh *= sh * sh;
+        t.S = p.dt * p.Kspeed * sh * 1.0 * Hh / 2.0;
+        for (int k = 0; k < 8; ++k) t.o[k] = t.mk[k] ? t.S * t.dh[k] / t.bk : 0.0;
+        return t;
+    }
+
+    // thermal_erosion + thermal_transport, layer 0
+    void thermal(const std::vector<double>& b, std::vector<double>& out) const {
+        const size_t c = (size_t)n * n;
+        std::vector<double> o(8 * c);
+        for (int y = 0; y < n; ++y)
+            for (int x = 0; x < n; ++x) {
+                Talus t = talus(b, x, y);
+                for (int k = 0; k < 8; ++k) o[8 * id(x, y) + k] = t.o[k];
+            }
+        const int opp[8] = {1, 0, 3, 2, 7, 6, 5, 4};
+        for (int y = 0; y < n; ++y)
+            for (int x = 0; x < n; ++x) {
+                size_t i = id(x, y);
+                double in_flux = 0;
+                for (int k = 0; k < 8; ++k) {
+                    int xx = x + TOX[k], yy = y + TOY[k];
+                    in_flux += in(xx, yy) ? o[8 * id(xx, yy) + opp[k]] : 0.0;
+                }
+                double sum = 0;
+                for (int k = 0; k < 8; ++k) sum -= o[8 * i + k];
+                sum += in_flux;
+                out[i] = b[i] + sum;
+            }
+    }
+
+    // Reverse of the thermal passes: A_out is d(loss)/d(rock after thermal),
+    // G receives d(loss)/d(rock before thermal).
+    void thermal_reverse(const std::vector<double>& b, const std::vector<double>& A_out,
+                         std::vector<double>& G) const {
+        const size_t c = (size_t)n * n;
+        G = A_out;
+        for (int y = 0; y < n; ++y)
+            for (int x = 0; x < n; ++x) {
+                Talus t = talus(b, x, y);
+                if (t.bk == 0.0) continue;  // no marked direction
+                size_t i = id(x, y);
+                double gk[8], gavg = 0;
+                for (int k = 0; k < 8; ++k) {
+                    gk[k] = 0;
+                    if (!t.mk[k]) continue;
+                    gk[k] = A_out[id(x + TOX[k], y + TOY[k])] - A_out[i];
+                    gavg += gk[k] * t.dh[k];
+                }
+                gavg /= t.bk;
+                double gdh[8] = {0, 0, 0, 0, 0, 0, 0, 0}, gb = 0;
+                for (int k = 0; k < 8; ++k)
+                    if (t.mk[k]) gdh[k] = t.S / t.bk * (gk[k] - gavg);
+                const double dS = gavg;
+                const double sh3 = t.s1 * t.s1 * t.s1;
+                const double Hh = gmin(b[i], t.Hmax);
+                const double dH = dS * p.dt * p.Kspeed * sh3 / 2.0;
+                if (t.sharp_taken && t.js >= 0) {
+                    double ds1 = dS * p.dt * p.Kspeed * Hh / 2.0 * 3.0 * t.s1 * t.s1;
+                    double dslope = ds1 / (1.0 + t.slope * t.slope);
+                    gdh[t.js] += dslope / (t.js >= 4 ? std::sqrt(2.0) : 1.0);
+                }
+                if (t.Hmax < b[i]) { if (t.jh >= 0) gdh[t.jh] += dH; }
+                else gb += dH;
+                double own = gb;
+                for (int k = 0; k < 8; ++k) {
+                    own += gdh[k];
+                    int xx = x + TOX[k], yy = y + TOY[k];
+                    if (in(xx, yy)) G[id(xx, yy)] -= gdh[k];
+                }
+                G[i] += own;
+            }
+        (void)c;
     }
 
     // Reverse of one step: A holds d(loss)/d(outputs of the step) and is
@@ -141,6 +260,9 @@ struct Model {
         R.init(c);
         std::vector<double> dse(c, 0), du(c, 0), dv(c, 0), dvz(c, 0), dd2(c, 0), ddr(c, 0);
         const double evap = 1 - p.Ke * p.dt;
+        // thermal: the adjoint of the eroded rock
+        std::vector<double> Abe = A.b;
+        if (p.Kspeed != 0.0) thermal_reverse(I.be, A.b, Abe);
         // sediment transport
         for (int y = 0; y < n; ++y)
             for (int x = 0; x < n; ++x) {
@@ -189,7 +311,7 @@ struct Model {
                 double craw = p.Kc * sa * ero;
                 double cc = gmax(0.0, craw);
                 double Kls = p.dt * (double)ks[i], Kld = p.dt * p.Kd0, b = X.b[i], s = X.s[i];
-                double ab = A.b[i], as = dse[i];
+                double ab = Abe[i], as = dse[i];
                 double gb = 0, gs = 0, gc = 0, gK = 0;
                 if (cc > s) {
                     double del = Kls * (cc - s);
@@ -305,14 +427,16 @@ struct Model {
 
 extern "C" {
 
-// settings: dt, G, ENERGY_KEPT, Kc, Kd[0], Ke, rain amount (floats as the
-// UBO holds them), rain period.  Inputs n*n doubles/floats; outputs n*n doubles.
+// settings: dt, G, ENERGY_KEPT, Kc, Kd[0], Ke, rain amount, Kalpha[0],
+// Kspeed[0] (floats as the UBO holds them), rain period.  Inputs n*n
+// doubles/floats; outputs n*n doubles.
 int hgo_adjoint_ref(int n, const float* settings, int period, uint64_t step0, int nsteps, const double* b0,
                     const float* ks, const double* target, double* loss, double* dKs, double* db0) {
     if (n <= 0 || nsteps < 0) return -1;
     Model m;
     m.n = n;
-    m.p = Params{settings[0], settings[1], settings[2], settings[3], settings[4], settings[5], settings[6], period};
+    m.p = Params{settings[0], settings[1], settings[2], settings[3], settings[4],
+                 settings[5], settings[6], settings[7], settings[8], period};
     m.ks = ks;
     const size_t c = (size_t)n * n;
     std::vector<State> tape(nsteps + 1);
@@ -342,7 +466,8 @@ int hgo_forward_ref(int n, const float* settings, int period, uint64_t step0, in
                     const float* ks, double* b_out) {
     Model m;
     m.n = n;
-    m.p = Params{settings[0], settings[1], settings[2], settings[3], settings[4], settings[5], settings[6], period};
+    m.p = Params{settings[0], settings[1], settings[2], settings[3], settings[4],
+                 settings[5], settings[6], settings[7], settings[8], period};
     m.ks = ks;
     const size_t c = (size_t)n * n;
     State X, Y;

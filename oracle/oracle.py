@@ -250,12 +250,14 @@ lib.hgo_forward_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, cty
 
 
 def _adj_settings(s, amount):
-    return np.array([s.d_t, s.G, s.ENERGY_KEPT, s.Kc, s.Kd[0], s.Ke, amount], dtype=np.float32)
+    return np.array([s.d_t, s.G, s.ENERGY_KEPT, s.Kc, s.Kd[0], s.Ke, amount, s.Kalpha[0], s.Kspeed[0]],
+                    dtype=np.float32)
 
 
 def adjoint_ref(settings, amount, period, b0, ks, target, nsteps, step0=0):
     """FP64 reference: loss = mean((rock_final - target)^2) after nsteps of the
-    thermal-free single-material step; returns (loss, dL/dKs, dL/drock0)."""
+    single-material step (thermal layer 0 when Kspeed[0] != 0); returns
+    (loss, dL/dKs, dL/drock0)."""
     n = b0.shape[0]
     st = _adj_settings(settings, amount)
     b0 = np.ascontiguousarray(b0, dtype=np.float64)
