@@ -1,13 +1,20 @@
 """The FP64 reference adjoint (oracle/hg_adjoint_ref.cpp) against central
 finite differences of the oracle's own FP64 forward restatement of the GLSL
-passes (an independent implementation), eps = 1e-3, on 64 random cells, for
+passes (an independent implementation), eps = 1e-3 (1e-5 with thermal
+erosion, see EPS), on 64 random cells, for
 the gradients with respect to the initial rock heights and the per-cell
-rock solubility.  CPU only."""
+rock solubility; without and with thermal erosion (talus tan 0.65,
+slippage 0.3 on the uniform-rain physics).  CPU only."""
 import numpy as np
+import pytest
 
 import oracle as O
 
-N, STEPS, EPS = 32, 16, 1e-3
+N, STEPS = 32, 16
+# eps 1e-3 for the thermal-free step; with thermal erosion slippage settles
+# slopes onto the talus angle, where the loss has kinks closer than 1e-3
+# apart, so the check uses 1e-5 there
+EPS = {False: 1e-3, True: 1e-5}
 
 
 def setup():
@@ -18,49 +25,72 @@ def setup():
     return rng, b0, ks, target
 
 
-def oracle_loss(b0, ks, target):
+def settings(thermal):
+    s = O.settings_config1()
+    if thermal:
+        s.Kspeed[0] = 0.3
+    return s
+
+
+def oracle_loss(b0, ks, target, thermal=False):
     w = O.OracleWorld(N, 64)
     w.set("rock", b0)
     w.set_ks(ks)
-    s, o = O.workload("config1")
-    w.step(s, o, STEPS)
+    _, o = O.workload("config1")
+    w.step(settings(thermal), o, STEPS)
     return np.mean((w.get("rock") - target) ** 2)
 
 
-def test_reference_forward_is_the_oracle_forward():
+@pytest.mark.parametrize("thermal", [False, True])
+def test_reference_forward_is_the_oracle_forward(thermal):
     _, b0, ks, _ = setup()
     w = O.OracleWorld(N, 64)
     w.set("rock", b0)
     w.set_ks(ks)
-    s, o = O.workload("config1")
-    w.step(s, o, STEPS)
-    ref = O.forward_ref(O.settings_config1(), 0.01, 1, b0, ks, STEPS)
+    _, o = O.workload("config1")
+    w.step(settings(thermal), o, STEPS)
+    ref = O.forward_ref(settings(thermal), 0.01, 1, b0, ks, STEPS)
     assert np.array_equal(ref, w.get("rock"))
 
 
-def test_reference_adjoint_vs_finite_differences():
+@pytest.mark.parametrize("thermal", [False, True])
+def test_reference_adjoint_vs_finite_differences(thermal):
     rng, b0, ks, target = setup()
-    loss, dks, db0 = O.adjoint_ref(O.settings_config1(), 0.01, 1, b0, ks, target, STEPS)
-    assert abs(loss - oracle_loss(b0, ks, target)) <= 1e-12 * loss
+    s = settings(thermal)
+    loss, dks, db0 = O.adjoint_ref(s, 0.01, 1, b0, ks, target, STEPS)
+    assert abs(loss - oracle_loss(b0, ks, target, thermal)) <= 1e-12 * loss
     cells = rng.choice(N * N, size=64, replace=False)
     scale_b = np.abs(db0).max()
     scale_k = np.abs(dks).max()
+    l0 = oracle_loss(b0, ks, target, thermal)
+    eps = EPS[thermal]
+
+    def close(g, lp, lm, h, scale):
+        """Central difference; with thermal erosion also either one-sided
+        difference: slippage settles slopes onto the talus angle, where the
+        step has kinks, and a subgradient is one of the one-sided slopes."""
+        tol = lambda fd: abs(fd - g) <= 1e-3 * max(abs(fd), 1e-2 * scale)
+        if tol((lp - lm) / h):
+            return True
+        return thermal and (tol(2 * (lp - l0) / h) or tol(2 * (l0 - lm) / h))
+
     bad = []
     for c in cells:
         y, x = divmod(int(c), N)
         bp, bm = b0.copy(), b0.copy()
-        bp[y, x] += EPS
-        bm[y, x] -= EPS
-        fd = (oracle_loss(bp, ks, target) - oracle_loss(bm, ks, target)) / (2 * EPS)
-        if abs(fd - db0[y, x]) > 1e-3 * max(abs(fd), 1e-2 * scale_b):
-            bad.append(("rock", y, x, db0[y, x], fd))
+        bp[y, x] += eps
+        bm[y, x] -= eps
+        lp, lm = oracle_loss(bp, ks, target, thermal), oracle_loss(bm, ks, target, thermal)
+        if not close(db0[y, x], lp, lm, 2 * eps, scale_b):
+            bad.append(("rock", y, x, db0[y, x], (lp - lm) / (2 * eps)))
         kp, km = ks.copy(), ks.copy()
-        kp[y, x] += np.float32(EPS)
-        km[y, x] -= np.float32(EPS)
+        kp[y, x] += np.float32(eps)
+        km[y, x] -= np.float32(eps)
         h = float(kp[y, x]) - float(km[y, x])
-        fd = (oracle_loss(b0, kp, target) - oracle_loss(b0, km, target)) / h
-        if abs(fd - dks[y, x]) > 1e-3 * max(abs(fd), 1e-2 * scale_k):
-            bad.append(("ks", y, x, dks[y, x], fd))
-    # a central difference can straddle a dissolve/deposit or clamp switch;
-    # allow at most 2 of the 128 comparisons to do so
+        lp, lm = oracle_loss(b0, kp, target, thermal), oracle_loss(b0, km, target, thermal)
+        if not close(dks[y, x], lp, lm, h, scale_k):
+            bad.append(("ks", y, x, dks[y, x], (lp - lm) / h))
+    # a difference can still straddle a dissolve/deposit, clamp or talus
+    # switch; allow at most 2 of the 128 comparisons to do so
+    print(f"thermal={thermal} eps={eps}: {len(bad)} of 128 outside 1e-3", bad[:3])
     assert len(bad) <= 2, bad[:5]
