@@ -184,6 +184,7 @@ __device__ __forceinline__ void adj_tile(const AdjCellArgs& a, float* sm, uint64
     const size_t i = (size_t)y * n + x;
     float ab, ad, af[4];
     adj_view_at(a.A, n, x, y, i, ab, ad, af);
+    if (a.gbe) ab = a.gbe[i];  // thermal on: the eroded rock's adjoint (k_adj_thermal)
     const float as = a.dse[i];
     const float DUs = a.du[i], DVs = a.dv[i];
     const float Ks_i = c.ks_field ? c.ks_field[i] : c.Ks0;
@@ -371,6 +372,168 @@ __global__ void k_adj_final(int n, AdjView A, float* __restrict__ out_b) {
     out_b[i] = ab;
 }
 
+// ---- k_adj_thermal ---------------------------------------------------------------
+// Reverse of thermal_erosion + thermal_transport (layer 0): from the adjoint
+// A of the rock after the talus passes to the adjoint G of the eroded rock.
+// rock' = b + sum_k in_k - sum_k o_k, o_k = S dh_k / bk for the marked
+// directions, S = dt Kspeed sharp^3 H / 2.  With g_k = A(neighbour k) - A(c):
+//   dL/ddh_j = S/bk (g_j - gbar) for marked j, gbar = sum_k g_k dh_k / bk
+//   dL/dS = gbar; H = min(b, max dh) and the steepest marked slope pass
+//   their derivative to the direction that attains them (the first one in
+//   direction order); the marks themselves are locally constant.
+// dh_j = b(c) - b(neighbour j): +dL/ddh_j to the cell, - to the neighbour.
+// 64 x 8 tiles; the per-cell terms of the tile and its one-cell ring go
+// through shared memory, from TMA boxes of the eroded rock and A with a
+// two-cell halo.
+constexpr int TT_H = 8, TT_NTH = 256;
+constexpr int TT_RW = TW + 2 * HX, TT_BH = TT_H + 4, TT_BOX = TT_RW * TT_BH;
+constexpr int TT_BRC = ((TT_BOX + 31) / 32) * 32;
+constexpr int TT_CW = TW + 2, TT_CH = TT_H + 2, TT_NC = TT_CW * TT_CH;  // tile + ring
+// direction k = L, R, T, B, LT, RT, LB, RB -> offset
+__host__ __device__ constexpr int tt_ox(int k) { return (k == 0 || k == 4 || k == 6) ? -1 : (k == 1 || k == 5 || k == 7) ? 1 : 0; }
+__host__ __device__ constexpr int tt_oy(int k) { return (k == 2 || k == 4 || k == 5) ? 1 : (k == 3 || k == 6 || k == 7) ? -1 : 0; }
+
+struct ThermalArgs {
+    CUtensorMap map_b;  // eroded rock of the step (box TT_RW x TT_BH)
+    CUtensorMap map_a;  // gathered adjoint of the step's output rock (same box)
+    StepConsts c;
+    const float* a;     // the same adjoint (global)
+    float* g;           // out: adjoint of the eroded rock
+};
+
+template <bool EDGE>
+__device__ __forceinline__ void thermal_tile(const ThermalArgs& ta, float* bs, float* as, float* gd, uint64_t* bar,
+                                             int tx0, int ty0, int* err) {
+    const StepConsts& c = ta.c;
+    const int n = c.n, tid = threadIdx.x;
+    const int gx0 = tx0 - HX, gy0 = ty0 - 2;
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, 2 * TT_BOX * sizeof(float));
+        tma_load_2d(bs, &ta.map_b, gx0, gy0, bar);
+        tma_load_2d(as, &ta.map_a, gx0, gy0, bar);
+    }
+    bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+        mbar_wait(bar, 0);
+        return;
+    }
+    // per-cell terms of the tile and its ring: gd[k * TT_NC + q] = dL/ddh_k,
+    // gd[8 * TT_NC + q] = the cell's own term (dL/db through H, plus sum_k dL/ddh_k)
+#pragma unroll 1
+    for (int q = tid; q < TT_NC; q += TT_NTH) {
+        const int rx = q % TT_CW - 1, ry = q / TT_CW - 1;
+        const int x = tx0 + rx, y = ty0 + ry;
+        float gdh[8] = {0, 0, 0, 0, 0, 0, 0, 0}, own = 0.0f;
+        if (!EDGE || (x >= 0 && x < n && y >= 0 && y < n)) {
+            const int si = (ry + 2) * TT_RW + HX + rx;
+            const float b = bs[si];
+            float dh[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                bool out = EDGE && (x + tt_ox(k) < 0 || x + tt_ox(k) >= n || y + tt_oy(k) < 0 || y + tt_oy(k) >= n);
+                dh[k] = b - (out ? FAR_HEIGHT : bs[si + tt_oy(k) * TT_RW + tt_ox(k)]);
+            }
+            // the forward's values (cell_thermal_outflows' operations)
+            float Hmax = 0.0f;
+            int jh = -1;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (dh[k] > Hmax) { Hmax = dh[k]; jh = k; }
+            const float H = gmin(b, Hmax);
+            float bk = 0.0f, max_cross = 0.0f, max_diag = 0.0f;
+            int jc = -1, jd = -1;
+            bool mk[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                mk[k] = dh[k] >= (k < 4 ? c.talus_x_cross : c.talus_b_diag);
+                if (mk[k]) {
+                    bk += dh[k];
+                    if (k < 4) { if (dh[k] > max_cross) { max_cross = dh[k]; jc = k; } }
+                    else if (dh[k] > max_diag) { max_diag = dh[k]; jd = k; }
+                }
+            }
+            if (bk > 0.0f) {
+                const float sd = max_diag / SQRT2_F;
+                const float slope = fmaxf(max_cross, sd);
+                const int js = (jd >= 0 && sd > max_cross) ? jd : jc;
+                const float alph = poly_atanf(slope);
+                float s1 = 1.0f;
+                const float newsh = 1.0f + alph - c.Kalpha0;
+                const bool taken = newsh > s1;
+                if (taken) s1 = newsh;
+                const float sh3 = s1 * (s1 * s1);
+                const float S = c.dt * c.Kspeed0 * sh3 * H / 2.0f;
+                // reverse
+                const float ac = as[si];
+                const float rbk = __frcp_rn(bk);
+                float g[8], gbar = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    g[k] = mk[k] ? as[si + tt_oy(k) * TT_RW + tt_ox(k)] - ac : 0.0f;
+                    gbar += g[k] * dh[k];
+                }
+                gbar *= rbk;
+                const float sb = S * rbk;
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (mk[k]) gdh[k] = sb * (g[k] - gbar);
+                const float dH = gbar * (c.dt * c.Kspeed0 * sh3 * 0.5f);
+                if (taken && js >= 0) {
+                    const float ds1 = gbar * (c.dt * c.Kspeed0 * H * 0.5f) * 3.0f * s1 * s1;
+                    const float dslope = ds1 * __frcp_rn(1.0f + slope * slope);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)  // static indices keep gdh in registers
+                        if (k == js) gdh[k] += k < 4 ? dslope : dslope * RCP_SQRT2_F;
+                }
+                if (Hmax < b) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (k == jh) gdh[k] += dH;
+                } else {
+                    own += dH;
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) own += gdh[k];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) gd[k * TT_NC + q] = gdh[k];
+        gd[8 * TT_NC + q] = own;
+    }
+    __syncthreads();
+    // G(c) = A(c) + own(c) - sum over neighbours m of m's dL/ddh toward c
+#pragma unroll 1
+    for (int q = tid; q < TW * TT_H; q += TT_NTH) {
+        const int ix = q % TW, iy = q / TW;
+        const int x = tx0 + ix, y = ty0 + iy;
+        const int rq = (iy + 1) * TT_CW + ix + 1;
+        float gsum = ta.a[(size_t)y * n + x] + gd[8 * TT_NC + rq];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int xx = x + tt_ox(k), yy = y + tt_oy(k);
+            if (EDGE && (xx < 0 || xx >= n || yy < 0 || yy >= n)) continue;
+            gsum -= gd[(k ^ (k < 4 ? 1 : 3)) * TT_NC + rq + tt_oy(k) * TT_CW + tt_ox(k)];  // opposite direction
+        }
+        ta.g[(size_t)y * n + x] = gsum;
+    }
+}
+
+__global__ void __launch_bounds__(TT_NTH) k_adj_thermal(const __grid_constant__ ThermalArgs ta, int* err) {
+    __shared__ __align__(128) float bs[TT_BRC];
+    __shared__ __align__(128) float as[TT_BRC];
+    __shared__ float gd[9 * TT_NC];
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    const int n = ta.c.n;
+    const int tiles_x = n / TW;
+    const int tx0 = (blockIdx.x % tiles_x) * TW, ty0 = (blockIdx.x / tiles_x) * TT_H;
+    bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 2 >= 0 && ty0 + TT_H + 2 <= n;
+    if (inner) thermal_tile<false>(ta, bs, as, gd, &bar, tx0, ty0, err);
+    else thermal_tile<true>(ta, bs, as, gd, &bar, tx0, ty0, err);
+}
+
 // d(mean((rock - target)^2))/d rock, and the loss partials
 __global__ void k_mse_grad(const float* __restrict__ b, const float* __restrict__ target, size_t count,
                            float* __restrict__ grad, double* __restrict__ part) {
@@ -421,6 +584,20 @@ void launch_adjoint_cell(const AdjCellArgs& args, int* err, cudaStream_t st) {
 
 void launch_adjoint_final(int n, const AdjView& A, float* out_b, cudaStream_t st) {
     k_adj_final<<<grid_for(n), dim3(BX, BY), 0, st>>>(n, A, out_b);
+    count_launch();
+}
+
+int adjoint_thermal_box_rows() { return TT_BH; }
+
+void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const CUtensorMap& map_a,
+                            const float* a, float* g, int* err, cudaStream_t st) {
+    ThermalArgs ta;
+    ta.map_b = map_b;
+    ta.map_a = map_a;
+    ta.c = c;
+    ta.a = a;
+    ta.g = g;
+    k_adj_thermal<<<(c.n / TW) * (c.n / TT_H), TT_NTH, 0, st>>>(ta, err);
     count_launch();
 }
 

@@ -242,7 +242,7 @@ bool thermal_on(const hg_world* w) {
 
 StepConsts make_consts(const hg_world* w);
 // the reversed step covers rain, flux, erosion and sediment transport
-bool adjoint_covers(const hg_world* w) { return !thermal_on(w) && make_consts(w).smooth_m == 0.0f; }
+bool adjoint_covers(const hg_world* w) { return make_consts(w).smooth_m == 0.0f; }
 
 StepConsts make_consts(const hg_world* w) {
     StepConsts c{};
@@ -1059,10 +1059,10 @@ struct hg_tape {
     float* ckpt = nullptr;   // nseg states: the input of each segment's first step
     float* seg = nullptr;    // K states: slot j >= 1 the input of a segment's step j,
                              // slot 0 receives the (unused) output of its last step
-    float* slots = nullptr;  // K x (u, v, eroded sediment) of a segment's steps
+    float* slots = nullptr;  // K x (u, v, eroded sediment, eroded rock) of a segment's steps
     float* adj = nullptr;    // 2 adjoint states (own terms), alternating A / R
     float* pk = nullptr;     // their 2 x ADJ_PACKET_FIELDS neighbour packets
-    float* aux = nullptr;    // 2 sediment-adjoint buffers, du, dv, eroded-rock scratch
+    float* aux = nullptr;    // 2 sediment-adjoint buffers, du, dv, rock adjoints for the talus reverse
     float* dks = nullptr;    // per-cell Ks gradient
     unsigned long long* d_step = nullptr;  // step counter of the recompute launches
     TmaCache tma;
@@ -1070,8 +1070,8 @@ struct hg_tape {
 
 namespace {
 constexpr int kStateFields = 7;
-constexpr int kSlotFields = 3;
-constexpr int kAuxFields = 5;
+constexpr int kSlotFields = 4;  // u, v, eroded sediment, eroded rock
+constexpr int kAuxFields = 6;   // 2 sediment-adjoint buffers, du, dv, gathered rock adjoint, eroded-rock adjoint
 
 AdjFields fields_at(float* base, size_t c) {
     AdjFields f;
@@ -1107,7 +1107,7 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     if (!out) return fail(HG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (nsteps < 1) return fail(HG_ERR_INVALID, "nsteps must be >= 1");
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion and smoothing");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without smoothing (Kspeed[1] == 0)");
     if (!fused_tile_ok(w->n, 16) || !adjoint_tile_ok(w->n))
         return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
     DeviceGuard g(w->device);
@@ -1175,7 +1175,6 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
     TerrainSrc src{};
     src.c = cst;
     src.rain = make_rain_base(w);
-    src.b_ero = t->aux + 4 * c;
     src.step = t->d_step;
     TerrainDesc td;
     for (int j = 0; j < len; ++j) {
@@ -1189,6 +1188,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
         src.u = sl;
         src.v = sl + c;
         src.s_ero = sl + 2 * c;
+        src.b_ero = sl + 3 * c;
         if (!fill_desc(td, src, th, 0, t->tma))
             return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
         launch_fused_one(td, th, w->err, w->stream);
@@ -1200,7 +1200,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
 int hg_forward(hg_tape* t) {
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     hg_world* w = t->w;
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion and smoothing");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without smoothing (Kspeed[1] == 0)");
     DeviceGuard g(w->device);
     t->step0 = w->step;
     const size_t c = cells(w);
@@ -1235,7 +1235,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
     if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
     hg_world* w = t->w;
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without thermal erosion and smoothing");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without smoothing (Kspeed[1] == 0)");
     DeviceGuard g(w->device);
     cudaStream_t st = w->stream;
     const size_t c = cells(w), sf = kStateFields * c;
@@ -1260,6 +1260,8 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     float* dse[2] = {t->aux, t->aux + c};
     float* du = t->aux + 2 * c;
     float* dv = t->aux + 3 * c;
+    float* abf = t->aux + 4 * c;  // gathered adjoint of the rock after the talus passes
+    float* gbe = t->aux + 5 * c;  // adjoint of the eroded rock
     // the final state's adjoint: rock only, no packets
     HG_CUDA(cudaMemsetAsync(t->adj, 0, 2 * sf * sizeof(float), st));
     HG_CUDA(cudaMemsetAsync(t->pk, 0, 2 * ADJ_PACKET_FIELDS * c * sizeof(float), st));
@@ -1294,6 +1296,17 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
             args.A = view(cur);
             args.dse = dse[m & 1];
             args.dse_prev = dse[(m + 1) & 1];
+            args.gbe = nullptr;
+            if (cst.thermal) {  // reverse the talus passes first: A's rock -> eroded rock's adjoint
+                launch_adjoint_final(w->n, view(cur), abf, st);
+                CUtensorMap mb, ma;
+                const float* be = slot_of(j).u + 3 * c;
+                if (!t->tma.get(be, w->n, adjoint_thermal_box_rows(), &mb) ||
+                    !t->tma.get(abf, w->n, adjoint_thermal_box_rows(), &ma))
+                    return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
+                launch_adjoint_thermal(cst, mb, ma, abf, gbe, w->err, st);
+                args.gbe = gbe;
+            }
             args.scatter_prev = j > 0 ? 1 : 0;
             args.prev = j > 0 ? slot_of(j - 1) : AdjSlot{nullptr, nullptr, nullptr};
             const AdjFields& R = own[cur ^ 1];
