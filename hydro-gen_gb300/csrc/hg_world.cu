@@ -1057,14 +1057,17 @@ struct hg_tape {
     bool recorded = false;
     bool last_ready = false;  // the last segment's states and intermediates are in seg / slots
     float* ckpt = nullptr;   // nseg states: the input of each segment's first step
-    float* seg = nullptr;    // K states: slot j >= 1 the input of a segment's step j,
+    int nbuf = 1;            // segment buffers: 2 lets the next segment's recompute overlap a reverse sweep
+    float* seg = nullptr;    // nbuf x K states: slot j >= 1 the input of a segment's step j,
                              // slot 0 receives the (unused) output of its last step
-    float* slots = nullptr;  // K x (u, v, eroded sediment, eroded rock) of a segment's steps
+    float* slots = nullptr;  // nbuf x K x (u, v, eroded sediment, eroded rock) of a segment's steps
     float* adj = nullptr;    // 2 adjoint states (own terms), alternating A / R
     float* pk = nullptr;     // their 2 x ADJ_PACKET_FIELDS neighbour packets
     float* aux = nullptr;    // 2 sediment-adjoint buffers, du, dv, rock adjoints for the talus reverse
     float* dks = nullptr;    // per-cell Ks gradient
     unsigned long long* d_step = nullptr;  // step counter of the recompute launches
+    cudaStream_t rstream = nullptr;        // recompute stream (nbuf == 2)
+    cudaEvent_t ev_rec[2] = {}, ev_rev[2] = {};  // per buffer: recompute done, reverse sweep done
     TmaCache tma;
 };
 
@@ -1085,6 +1088,11 @@ AdjFields fields_at(float* base, size_t c) {
 void free_tape(hg_tape* t) {
     cudaFree(t->ckpt); cudaFree(t->seg); cudaFree(t->slots); cudaFree(t->adj); cudaFree(t->pk);
     cudaFree(t->aux); cudaFree(t->dks); cudaFree(t->d_step);
+    for (int b = 0; b < 2; ++b) {
+        if (t->ev_rec[b]) cudaEventDestroy(t->ev_rec[b]);
+        if (t->ev_rev[b]) cudaEventDestroy(t->ev_rev[b]);
+    }
+    if (t->rstream) cudaStreamDestroy(t->rstream);
 }
 
 // state fields of a world (current buffers) -> contiguous state at dst
@@ -1095,10 +1103,10 @@ int copy_state_out(hg_world* w, float* dst, cudaStream_t st) {
     return HG_OK;
 }
 
-size_t tape_bytes(size_t c, int nsteps, int K) {
+size_t tape_bytes(size_t c, int nsteps, int K, int nbuf) {
     const size_t nseg = (size_t)(nsteps + K - 1) / K;
-    return ((nseg + K) * kStateFields + (size_t)K * kSlotFields + 2 * kStateFields + 2 * ADJ_PACKET_FIELDS +
-            kAuxFields + 1) * c * sizeof(float);
+    return (nseg * kStateFields + (size_t)nbuf * K * (kStateFields + kSlotFields) + 2 * kStateFields +
+            2 * ADJ_PACKET_FIELDS + kAuxFields + 1) * c * sizeof(float);
 }
 }  // namespace
 
@@ -1112,26 +1120,47 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
         return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
     DeviceGuard g(w->device);
     const size_t c = cells(w);
-    int K = ckpt_every;
+    // Checkpoints (nsteps/K states) plus segment buffers (K states and
+    // slots each): K ~ sqrt(nsteps), two segment buffers when half the free
+    // memory holds them.  With HG_AUTO the interval nearest sqrt(nsteps)
+    // that fits is taken, two buffers first.
+    size_t free_b = 0, total_b = 0;
+    const size_t budget = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess ? free_b / 2 : (size_t)-1;
+    int K = ckpt_every, nbuf = 1;
     if (K == HG_AUTO || K <= 0) {
-        // checkpoints (nsteps/K states) plus segment buffers (K states and
-        // slots): ~sqrt(nsteps), fewer when half the free memory cannot hold it
-        K = (int)std::ceil(std::sqrt((double)nsteps));
-        size_t free_b = 0, total_b = 0;
-        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
-            while (K > 1 && tape_bytes(c, nsteps, K) > free_b / 2) --K;
+        const int K0 = std::min(nsteps, (int)std::ceil(std::sqrt((double)nsteps)));
+        K = 0;
+        for (int nb = 2; nb >= 1 && K == 0; --nb)
+            for (int d = 0; d < nsteps && K == 0; ++d)
+                for (int cand : {K0 - d, K0 + d})
+                    if (cand >= 1 && cand <= nsteps && tape_bytes(c, nsteps, cand, nb) <= budget) {
+                        K = cand;
+                        nbuf = nb;
+                        break;
+                    }
+        if (K == 0) K = K0;  // nothing fits: let the allocation report it
+    } else {
+        K = std::min(K, nsteps);
+        nbuf = tape_bytes(c, nsteps, K, 2) <= budget ? 2 : 1;
     }
-    K = std::min(K, nsteps);
     hg_tape* t = new (std::nothrow) hg_tape();
     if (!t) return fail(HG_ERR_OOM, "host allocation failed");
     t->w = w;
     t->nsteps = nsteps;
     t->K = K;
     t->nseg = (nsteps + K - 1) / K;
+    t->nbuf = t->nseg > 1 ? nbuf : 1;
     const size_t fb = c * sizeof(float);
     cudaError_t e = cudaMalloc((void**)&t->ckpt, (size_t)t->nseg * kStateFields * fb);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&t->seg, (size_t)K * kStateFields * fb);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&t->slots, (size_t)K * kSlotFields * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->seg, (size_t)t->nbuf * K * kStateFields * fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->slots, (size_t)t->nbuf * K * kSlotFields * fb);
+    if (e == cudaSuccess && t->nbuf == 2) {
+        e = cudaStreamCreateWithFlags(&t->rstream, cudaStreamNonBlocking);
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+            e = cudaEventCreateWithFlags(&t->ev_rec[b], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t->ev_rev[b], cudaEventDisableTiming);
+        }
+    }
     if (e == cudaSuccess) e = cudaMalloc((void**)&t->adj, 2 * kStateFields * fb);
     if (e == cudaSuccess) e = cudaMalloc((void**)&t->pk, 2 * ADJ_PACKET_FIELDS * fb);
     if (e == cudaSuccess) e = cudaMalloc((void**)&t->aux, kAuxFields * fb);
@@ -1164,34 +1193,42 @@ int hg_tape_info(const hg_tape* t, int* nsteps, int* ckpt_every) {
     return HG_OK;
 }
 
-// Recomputes segment s from its checkpoint with the fused step: step j reads
-// its input state (checkpoint or seg slot j) and writes the next state into
-// seg slot j + 1 and u, v, eroded sediment into its slots; the last step's
-// state goes to `last_out` (7 fields) or seg slot 0.  No state copies.
-int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th, float* const* last_out) {
+// Segment buffer b: its K states and K slot groups.
+float* seg_buf(hg_tape* t, int b) { return t->seg + (size_t)b * t->K * kStateFields * cells(t->w); }
+float* slot_buf(hg_tape* t, int b) { return t->slots + (size_t)b * t->K * kSlotFields * cells(t->w); }
+
+// Recomputes segment s from its checkpoint with the fused step on stream
+// `st` into segment buffer b: step j reads its input state (checkpoint or
+// state slot j) and writes the next state into state slot j + 1 and u, v,
+// eroded sediment and eroded rock into its slot group; the last step's state
+// goes to `last_out` (7 fields) or state slot 0.  No state copies.
+int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th, float* const* last_out, int b,
+                      cudaStream_t st) {
     hg_world* w = t->w;
     const size_t c = cells(w), sf = kStateFields * c;
-    k_set_u64<<<1, 1, 0, w->stream>>>(t->d_step, (unsigned long long)(t->step0 + (uint64_t)s * t->K));
+    float* segb = seg_buf(t, b);
+    float* slotb = slot_buf(t, b);
+    k_set_u64<<<1, 1, 0, st>>>(t->d_step, (unsigned long long)(t->step0 + (uint64_t)s * t->K));
     TerrainSrc src{};
     src.c = cst;
     src.rain = make_rain_base(w);
     src.step = t->d_step;
     TerrainDesc td;
     for (int j = 0; j < len; ++j) {
-        const float* in = j == 0 ? t->ckpt + (size_t)s * sf : t->seg + (size_t)j * sf;
-        float* outp = t->seg + (size_t)(j + 1 < len ? j + 1 : 0) * sf;
+        const float* in = j == 0 ? t->ckpt + (size_t)s * sf : segb + (size_t)j * sf;
+        float* outp = segb + (size_t)(j + 1 < len ? j + 1 : 0) * sf;
         for (int f = 0; f < S_COUNT; ++f) {
             src.in[f] = in + f * c;
             src.out[f] = (j + 1 == len && last_out) ? last_out[f] : outp + f * c;
         }
-        float* sl = t->slots + (size_t)j * kSlotFields * c;
+        float* sl = slotb + (size_t)j * kSlotFields * c;
         src.u = sl;
         src.v = sl + c;
         src.s_ero = sl + 2 * c;
         src.b_ero = sl + 3 * c;
         if (!fill_desc(td, src, th, 0, t->tma))
             return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
-        launch_fused_one(td, th, w->err, w->stream);
+        launch_fused_one(td, th, w->err, st);
     }
     HG_CUDA(cudaGetLastError());
     return HG_OK;
@@ -1216,12 +1253,12 @@ int hg_forward(hg_tape* t) {
         // the last segment steps through the tape's buffers: its states and
         // intermediates stay for the backward sweep, the final state lands in
         // the world's alternate buffers
-        rc = recompute_segment(t, s, len, make_consts(w), w->tuning.th ? w->tuning.th : 16, w->alt);
+        rc = recompute_segment(t, s, len, make_consts(w), w->tuning.th ? w->tuning.th : 16, w->alt, 0, w->stream);
         if (rc != HG_OK) return rc;
         for (int f = 0; f < S_COUNT; ++f) std::swap(w->cur[f], w->alt[f]);
         w->step += (uint64_t)len;
         w->dev_step_valid = false;
-        const float* sl = t->slots + (size_t)(len - 1) * kSlotFields * c;
+        const float* sl = slot_buf(t, 0) + (size_t)(len - 1) * kSlotFields * c;
         HG_CUDA(cudaMemcpyAsync(w->u, sl, c * sizeof(float), cudaMemcpyDeviceToDevice, w->stream));
         HG_CUDA(cudaMemcpyAsync(w->v, sl + c, c * sizeof(float), cudaMemcpyDeviceToDevice, w->stream));
     }
@@ -1268,10 +1305,33 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     HG_CUDA(cudaMemsetAsync(t->aux, 0, 2 * c * sizeof(float), st));  // scatter targets start at zero
     HG_CUDA(cudaMemcpyAsync(own[0].b, dL_drock_final, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
     HG_CUDA(cudaMemsetAsync(t->dks, 0, c * sizeof(float), st));
+    // segment s lives in buffer (nseg - 1 - s) % nbuf; with two buffers the
+    // next segment's recompute runs on the recompute stream while this
+    // segment's reverse sweep runs on the world's stream
+    const bool overlap = t->nbuf == 2;
+    auto buf_of = [&](int s) { return overlap ? (t->nseg - 1 - s) & 1 : 0; };
+    int bcur = 0;
     auto slot_of = [&](int j) {
-        const float* sl = t->slots + (size_t)j * kSlotFields * c;
+        const float* sl = slot_buf(t, bcur) + (size_t)j * kSlotFields * c;
         return AdjSlot{sl, sl + c, sl + 2 * c};
     };
+    auto recompute = [&](int s, cudaStream_t rs) -> int {
+        const int b = buf_of(s);
+        if (overlap) HG_CUDA(cudaStreamWaitEvent(rs, t->ev_rev[b], 0));  // the sweep that used b is done
+        int rc = recompute_segment(t, s, std::min(t->K, t->nsteps - s * t->K), cst, th, nullptr, b, rs);
+        if (rc != HG_OK) return rc;
+        if (overlap) HG_CUDA(cudaEventRecord(t->ev_rec[b], rs));
+        return HG_OK;
+    };
+    if (overlap) {
+        // the recompute stream starts after everything queued on the world's stream
+        HG_CUDA(cudaEventRecord(t->ev_rev[0], st));
+        HG_CUDA(cudaEventRecord(t->ev_rev[1], st));
+    }
+    if (!t->last_ready) {  // the forward left the last segment in buffer 0 otherwise
+        int rc = recompute(t->nseg - 1, overlap ? t->rstream : st);
+        if (rc != HG_OK) return rc;
+    }
     AdjCellArgs args;
     args.c = cst;
     args.du = du;
@@ -1281,14 +1341,21 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     uint64_t m = 0;   // reversed steps so far: step m uses dse[m & 1]
     for (int s = t->nseg - 1; s >= 0; --s) {
         const int len = std::min(t->K, t->nsteps - s * t->K);
-        if (!(s + 1 == t->nseg && t->last_ready)) {  // the forward left the last segment in place
-            int rc = recompute_segment(t, s, len, cst, th, nullptr);
+        bcur = buf_of(s);
+        if (overlap) {
+            HG_CUDA(cudaStreamWaitEvent(st, t->ev_rec[bcur], 0));
+            if (s > 0) {  // the previous segment into the other buffer, concurrently
+                int rc = recompute(s - 1, t->rstream);
+                if (rc != HG_OK) return rc;
+            }
+        } else if (s + 1 < t->nseg) {
+            int rc = recompute(s, st);
             if (rc != HG_OK) return rc;
         }
         // the segment's last step: its sediment pass reversed on its own
         launch_adjoint_sediment(cst, slot_of(len - 1), own[cur].s, dse[m & 1], du, dv, st);
         for (int j = len - 1; j >= 0; --j, ++m) {
-            const float* xin = j == 0 ? t->ckpt + (size_t)s * sf : t->seg + (size_t)j * sf;
+            const float* xin = j == 0 ? t->ckpt + (size_t)s * sf : seg_buf(t, bcur) + (size_t)j * sf;
             for (int f = 0; f < kStateFields; ++f)
                 if (!t->tma.get(xin + f * c, w->n, adjoint_box_rows(), &args.maps[f]))
                     return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
@@ -1324,8 +1391,9 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
             launch_adjoint_cell(args, w->err, st);
             cur ^= 1;
         }
+        if (overlap) HG_CUDA(cudaEventRecord(t->ev_rev[bcur], st));
     }
-    if (t->nseg > 1) t->last_ready = false;  // other segments' recomputes reused the buffers
+    if (t->nseg > t->nbuf) t->last_ready = false;  // other segments' recomputes reused buffer 0
     if (dL_drock0) launch_adjoint_final(w->n, view(cur), dL_drock0, st);
     if (dL_dks) HG_CUDA(cudaMemcpyAsync(dL_dks, t->dks, c * sizeof(float), cudaMemcpyDeviceToDevice, st));
     HG_CUDA(cudaGetLastError());
