@@ -303,26 +303,25 @@ __device__ __forceinline__ void cell_thermal_outflows(const StepConsts& c, float
     float dh[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];
+    // H only matters when a direction is marked, i.e. some drop is >= a
+    // positive threshold: then the shader's "if (dh > H) H = dh" from 0 and
+    // fmaxf agree (NaN drops are skipped by both)
     float H = 0.0f;
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (dh[k] > H) H = dh[k];
+    for (int k = 0; k < 8; ++k) H = fmaxf(H, dh[k]);
     H = gmin(b, H);
-    float bk = 0.0f, max_cross = 0.0f, max_diag = 0.0f;
-    bool mk[8], any = false;
+    // marked drops (0 where unmarked): sums and maxima over the marked set
+    float dm[8], bk = 0.0f, max_cross = 0.0f, max_diag = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        mk[k] = dh[k] >= (k < 4 ? c.talus_x_cross : c.talus_b_diag);
-        if (mk[k]) {
-            bk += dh[k];
-            any = true;
-            if (k < 4) max_cross = fmaxf(max_cross, dh[k]);
-            else max_diag = fmaxf(max_diag, dh[k]);
-        }
+        dm[k] = dh[k] >= (k < 4 ? c.talus_x_cross : c.talus_b_diag) ? dh[k] : 0.0f;
+        bk += dm[k];  // + 0 leaves the sum's bits unchanged (it starts at +0)
+        if (k < 4) max_cross = fmaxf(max_cross, dm[k]);
+        else max_diag = fmaxf(max_diag, dm[k]);
     }
 #pragma unroll
     for (int k = 0; k < 8; ++k) o[k] = 0.0f;
-    if (!any) return;
+    if (!(bk > 0.0f)) return;  // no marked direction (marked drops are > 0)
     bool fast = c.fast_div && bk <= 0x1p40f;  // then max_diag is 0 or in [2^-30, 2^40]
     const float sd = fast ? div_recip(max_diag, SQRT2_F, RCP_SQRT2_F) : max_diag / SQRT2_F;
     const float alph = poly_atanf(fmaxf(max_cross, sd));
@@ -333,14 +332,15 @@ __device__ __forceinline__ void cell_thermal_outflows(const StepConsts& c, float
     const float S = c.dt * c.Kspeed0 * sharp * H / 2.0f;  // a == L == 1
     fast = fast && S >= 0x1p-50f && S <= 0x1p40f;
     if (fast) {
+        // S > 0: an unmarked direction's dividend S * 0 is +0 and its
+        // quotient +0, the shader's 0
         const float y = __frcp_rn(bk);
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (mk[k]) o[k] = div_recip(S * dh[k], bk, y);
+        for (int k = 0; k < 8; ++k) o[k] = div_recip(S * dm[k], bk, y);
     } else {
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-            if (mk[k]) o[k] = S * dh[k] / bk;
+            if (dm[k] != 0.0f) o[k] = S * dh[k] / bk;
     }
 }
 

@@ -350,32 +350,81 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
     }
     __syncthreads();
     // ---- thermal_transport: own outflows out, neighbours' outflows in -------
+    // (cell_thermal_apply's operations: in_flux = in[0] + ... + in[7] from 0,
+    // sum = 0 - own[0] - ... - own[7], rock = b + (sum + in_flux))
     {
         const int oi = (ry - 1) * RW + rx0;
-        float4 own4[8];
+        const float4 oL = ld4(outf + 0 * O_C + oi), oR = ld4(outf + 1 * O_C + oi);
+        float osum[4];
 #pragma unroll
-        for (int d = 0; d < 8; ++d) own4[d] = ld4(outf + d * O_C + oi);
-        // inflow from direction d = neighbour (dx, dy)'s outflow toward this cell
-        const float4 inT = ld4(outf + 3 * O_C + oi + RW);  // top neighbour's B
-        const float4 inB = ld4(outf + 2 * O_C + oi - RW);  // bottom neighbour's T
+        for (int j = 0; j < 4; ++j) {
+            osum[j] = 0.0f;
+            osum[j] -= at4(oL, j);
+            osum[j] -= at4(oR, j);
+        }
+#pragma unroll
+        for (int d = 2; d < 8; ++d) {
+            const float4 o = ld4(outf + d * O_C + oi);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) osum[j] -= at4(o, j);
+        }
+        // inflow from direction d = neighbour (dx, dy)'s outflow toward this
+        // cell.  Rows of outflows are read as aligned float4 (the group's own
+        // four columns); the column left (right) of the group comes from the
+        // neighbouring group in the warp, lane - 1 (+ 1), or at the tile edge
+        // from the ring column.
+        const unsigned FULL = 0xffffffffu;
+        const bool first = g == 0, last = g == GPR - 1;
+        float pR = __shfl_up_sync(FULL, oR.w, 1);
+        float nL = __shfl_down_sync(FULL, oL.x, 1);
+        if (first) pR = outf[1 * O_C + oi - 1];
+        if (last) nL = outf[0 * O_C + oi + 4];
+        float inf[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            inf[j] = 0.0f;
+            inf[j] += j == 0 ? pR : at4(oR, j - 1);  // L neighbour's R
+            inf[j] += j == 3 ? nL : at4(oL, j + 1);  // R neighbour's L
+        }
+        {
+            const float4 inT = ld4(outf + 3 * O_C + oi + RW);  // top neighbour's B
+            const float4 inB = ld4(outf + 2 * O_C + oi - RW);  // bottom neighbour's T
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                inf[j] += at4(inT, j);
+                inf[j] += at4(inB, j);
+            }
+        }
+        {
+            const float4 rbT = ld4(outf + 7 * O_C + oi + RW);  // row above: RB outflows
+            const float4 lbT = ld4(outf + 6 * O_C + oi + RW);  // row above: LB outflows
+            float pRB = __shfl_up_sync(FULL, rbT.w, 1);
+            float nLB = __shfl_down_sync(FULL, lbT.x, 1);
+            if (first) pRB = outf[7 * O_C + oi + RW - 1];
+            if (last) nLB = outf[6 * O_C + oi + RW + 4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                inf[j] += j == 0 ? pRB : at4(rbT, j - 1);  // LT neighbour's RB
+                inf[j] += j == 3 ? nLB : at4(lbT, j + 1);  // RT neighbour's LB
+            }
+        }
+        {
+            const float4 rtB = ld4(outf + 5 * O_C + oi - RW);  // row below: RT outflows
+            const float4 ltB = ld4(outf + 4 * O_C + oi - RW);  // row below: LT outflows
+            float pRT = __shfl_up_sync(FULL, rtB.w, 1);
+            float nLT = __shfl_down_sync(FULL, ltB.x, 1);
+            if (first) pRT = outf[5 * O_C + oi - RW - 1];
+            if (last) nLT = outf[4 * O_C + oi - RW + 4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                inf[j] += j == 0 ? pRT : at4(rtB, j - 1);  // LB neighbour's RT
+                inf[j] += j == 3 ? nLT : at4(ltB, j + 1);  // RB neighbour's LT
+            }
+        }
         const float4 b4 = ld4(be + ry * RW + rx0);
         float res[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int o = oi + j;
-            float own[8], in[8];
-#pragma unroll
-            for (int d = 0; d < 8; ++d) own[d] = at4(own4[d], j);
-            in[0] = outf[1 * O_C + o - 1];       // L neighbour's R
-            in[1] = outf[0 * O_C + o + 1];       // R neighbour's L
-            in[2] = at4(inT, j);                 // T neighbour's B
-            in[3] = at4(inB, j);                 // B neighbour's T
-            in[4] = outf[7 * O_C + o + RW - 1];  // LT neighbour's RB
-            in[5] = outf[6 * O_C + o + RW + 1];  // RT neighbour's LB
-            in[6] = outf[5 * O_C + o - RW - 1];  // LB neighbour's RT
-            in[7] = outf[4 * O_C + o - RW + 1];  // RB neighbour's LT
-            res[j] = cell_thermal_apply(at4(b4, j), own, in);
-        }
+        for (int j = 0; j < 4; ++j) res[j] = at4(b4, j) + (osum[j] + inf[j]);
         st4(td.out[S_ROCK] + gi0, make_float4(res[0], res[1], res[2], res[3]));
     }
 }
@@ -399,14 +448,14 @@ __device__ __forceinline__ void transport_block(const TerrainHot& td, const CUte
 }
 
 template <int TH>
-__global__ void __launch_bounds__(Geo<TH>::NTH) k_transport(const __grid_constant__ BatchParams bp,
+__global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport(const __grid_constant__ BatchParams bp,
                                                             const CUtensorMap* __restrict__ maps, int* err) {
     const int t = find_terrain(bp.tile0, bp.nterr, blockIdx.x);
     transport_block<TH>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
 }
 
 template <int TH>
-__global__ void __launch_bounds__(Geo<TH>::NTH) k_transport1(const __grid_constant__ TerrainDesc td, int* err) {
+__global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport1(const __grid_constant__ TerrainDesc td, int* err) {
     transport_block<TH>(td.h, td.maps, blockIdx.x, err);
 }
 
