@@ -56,6 +56,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(dist, value, device):
+    """The job's time for replicas: the slowest rank's (weak scaling)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world_size, cells, steps, seconds):
+    """Cell-steps per second of the whole job: every rank advances its own
+    world of `cells` cells by `steps` steps within `seconds`."""
+    return world_size * cells * steps / seconds
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -387,11 +403,7 @@ def main():
         e1.synchronize()
         launches = H.lib.hg_launch_count() - l0
         barrier()
-        ms = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(dist, e0.elapsed_time(e1), "cuda")
         return ms, launches
 
     # per-pass kernels (denominator of the fused-vs-plain ratio)
@@ -408,8 +420,8 @@ def main():
     # (two launches) that moves the step's 72 B per cell
     fused_step_ms = fused_ms / args.steps
 
-    value = world_size * cells * args.steps / (fused_ms / 1e3)
-    plain_value = world_size * cells * plain_steps / (plain_ms / 1e3)
+    value = job_throughput(world_size, cells, args.steps, fused_ms / 1e3)
+    plain_value = job_throughput(world_size, cells, plain_steps, plain_ms / 1e3)
 
     # e2e: C ABI with pinned host buffers, copies inside the timed region
     host = {f: torch.zeros((n, n), dtype=torch.float32).pin_memory() for f in H.STATE_FIELDS[:7]}
@@ -424,11 +436,7 @@ def main():
     for f, t in outs.items():
         H.check(H.lib.hg_world_download(w.h, H.FIELDS[f], t.data_ptr()))
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0, "cuda")
     h2d = 7 * cells * 4 / args.steps
     d2h = 3 * cells * 4 / args.steps
 
@@ -457,7 +465,7 @@ def main():
                      "algorithmic_bytes_per_step": BYTES_PER_CELL_STEP * cells},
         "clocks": clk.summary(),
         "gpu_launches": launches,
-        "e2e": {"value": world_size * cells * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": job_throughput(world_size, cells, args.steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
     }
     if not args.no_extras:
