@@ -130,6 +130,10 @@ struct StepConsts {
     float talus_b_diag;   // smallest positive height drop whose diagonal slope does
     int fast_div;         // both thresholds >= 2^-30: outflow quotients by div_recip
     float smooth_m;       // smoothing weight clamp(Kspeed[1]*d_t, 0, 1); 0: the pass is the identity
+    // two-layer worlds (rock + dirt)
+    float Ks1;            // Ks[1]
+    float Kconv;          // sediment conversion rock -> dirt
+    float Kalpha1, Kspeed1;
 };
 
 // ---- hydro_flux, glsl/hydro_flux.glsl:77-166 -------------------------------------
@@ -234,6 +238,59 @@ __device__ __forceinline__ void cell_erosion(const StepConsts& c, float Kls0, fl
     // :84-88 conversion with Kconv == 0 leaves s unchanged
 }
 
+// Two-layer form (rock r, dirt g; rock sediment s0, dirt sediment s1):
+// the shader's layer loop from dirt down to rock and the s0 -> s1
+// conversion.  Neighbours' heights are (rock, dirt) pairs, 0 outside.
+__device__ __forceinline__ void cell_erosion2(const StepConsts& c, float Kls0, float u, float v, float vz,
+                                              float& r, float& g, float& s0, float& s1,
+                                              float rr, float rg, float lr, float lg,
+                                              float tr, float tg, float br, float bg) {
+    float len = sqrtf(u * u + v * v);
+    float ero_vel = len;
+    if (vz < 1e-3f) {
+        float dd = gmax(5e-4f, vz);
+        float t = gclamp((dd - 1e-3f) / (5e-4f - 1e-3f), 0.0f, 1.0f);
+        t = t * t * (3.0f - 2.0f * t);
+        ero_vel = gmix(len, 0.0f, t);
+    }
+    // :23-35 (r.r + r.g) - l.r - l.g, likewise along y
+    float dx = rr + rg - lr - lg;
+    float dz = tr + tg - br - bg;
+    float cx = dx * 2.0f - 0.0f * dz;
+    float cy = 0.0f * 0.0f - 2.0f * 2.0f;
+    float cz = 2.0f * dz - dx * 0.0f;
+    float len3 = sqrtf(cx * cx + cy * cy + cz * cz);
+    float ny = cy / len3;
+    float sin_a = fabsf(sqrtf(1.0f - ny * ny));
+    float terr[2] = {r, g}, sed[2] = {s0, s1};
+    const float Kls[2] = {Kls0, c.Kls1}, Kld[2] = {c.Kld0, c.Kld1};
+    float cap = 0.0f;
+#pragma unroll
+    for (int i = 1; i >= 0; --i) {
+        float cc = gmax(0.0f, c.Kc * gmax(0.02f, sin_a) * ero_vel - cap);
+        if (cc > sed[i]) {
+            float old = terr[i];
+            terr[i] = terr[i] - Kls[i] * (cc - sed[i]);
+            sed[i] = sed[i] + Kls[i] * (cc - sed[i]);
+            if (terr[i] < 0.0f) {
+                sed[i] = sed[i] + terr[i];
+                terr[i] = 0.0f;
+                cap = cap + old;
+            } else {
+                break;
+            }
+        } else {
+            terr[i] = terr[i] + Kld[i] * (sed[i] - cc);
+            sed[i] = sed[i] - Kld[i] * (sed[i] - cc);
+        }
+    }
+    // :84-88 conversion of rock sediment into dirt sediment
+    float conv = sed[0] * c.Kconv * c.dt;
+    sed[1] = sed[1] + conv;
+    sed[0] = sed[0] - conv;
+    r = terr[0]; g = terr[1]; s0 = sed[0]; s1 = sed[1];
+}
+
 // ---- sediment_transport, glsl/sediment_transport.glsl:66-93 ----------------------
 // Back-trace point of the semi-Lagrangian step (:70, clamp :26-29).
 __device__ __forceinline__ void backtrace(const StepConsts& c, int x, int y, float u, float v,
@@ -260,16 +317,16 @@ __device__ __forceinline__ float bilinear_mix(float px, float py, float s00, flo
 // marked direction k is (S * dh_k) / bk.
 struct ThermalOut { float S, bk; uint32_t mask; };
 
-// Faithful form: one arctangent per downhill direction, as in the shader.
-__device__ __forceinline__ ThermalOut cell_thermal_ref(const StepConsts& c, float b, const float nb[8]) {
-    float dh[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];  // 0 + (b - nb) == b - nb
+// Faithful form: one arctangent per downhill direction, as in the shader,
+// for the drops dh[] (summed over the layers up to this one) and the layer's
+// own height `terr`, talus angle and slippage rate.
+__device__ __forceinline__ ThermalOut cell_thermal_dh(float dt, float Kalpha, float Kspeed, float terr,
+                                                      const float dh[8]) {
     float H = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         if (dh[k] > H) H = dh[k];
-    H = gmin(b, H);
+    H = gmin(terr, H);
     ThermalOut o{0.0f, 0.0f, 0u};
     float sharp = 1.0f;
 #pragma unroll
@@ -278,16 +335,24 @@ __device__ __forceinline__ ThermalOut cell_thermal_ref(const StepConsts& c, floa
         if (bb <= 0.0f) continue;
         float slope = k < 4 ? bb : bb / 1.41421354f;  // d = L (cross) or L*sqrt(2)
         float alph = poly_atanf(slope);
-        if (alph > c.Kalpha0) {
-            float newsh = 1.0f + alph - c.Kalpha0;
+        if (alph > Kalpha) {
+            float newsh = 1.0f + alph - Kalpha;
             if (newsh > sharp) sharp = newsh;
             o.bk += bb;
             o.mask |= 1u << k;
         }
     }
     sharp *= sharp * sharp;
-    o.S = c.dt * c.Kspeed0 * sharp * H / 2.0f;  // a == L == 1
+    o.S = dt * Kspeed * sharp * H / 2.0f;  // a == L == 1
     return o;
+}
+
+// Layer 0 (rock): drops b - nb (the shader's 0 + (b - nb)).
+__device__ __forceinline__ ThermalOut cell_thermal_ref(const StepConsts& c, float b, const float nb[8]) {
+    float dh[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];
+    return cell_thermal_dh(c.dt, c.Kalpha0, c.Kspeed0, b, dh);
 }
 
 // The shader's outflows with one arctangent per cell, written to o[8].
@@ -372,6 +437,31 @@ __device__ __forceinline__ float cell_smooth(float m, float tr, float lr, float 
     if (((-dl > hdiff || -dr > hdiff) && xs > 0.0f) || ((-dt_ > hdiff || -db > hdiff) && ys > 0.0f))
         nr = (tr + lr + rr + tt + bt) / 5.0f;
     return m * nr + (1.0f - m) * tr;
+}
+
+// Two-layer smoothing (rock r, dirt g; neighbours left, right, top (y+1),
+// bottom (y-1)): the dirt differences include the rock differences.
+__device__ __forceinline__ void cell_smooth2(float m, float& tr, float& tg, float lr, float lg, float rr, float rg,
+                                             float ttr, float ttg, float bbr, float bbg) {
+    float dlr = tr - lr, dlg = tg - lg;
+    dlg += dlr;
+    float drr = tr - rr, drg = tg - rg;
+    drg += drr;
+    float dtr = tr - ttr, dtg = tg - ttg;
+    dtg += dtr;
+    float dbr = tr - bbr, dbg = tg - bbg;
+    dbg += dbr;
+    float g_hdiff = fabsf((dlg + drg + dtg + dbg) / 4.0f);
+    float r_hdiff = fabsf((dlr + drr + dtr + dbr) / 4.0f);
+    float xr = dlr * drr, xg = dlg * drg;
+    float yr = dtr * dbr, yg = dtg * dbg;
+    float nr = tr, ng = tg;
+    if (((-dlr > r_hdiff || -drr > r_hdiff) && xr > 0.0f) || ((-dtr > r_hdiff || -dbr > r_hdiff) && yr > 0.0f))
+        nr = (tr + lr + rr + ttr + bbr) / 5.0f;
+    if (((-dlg > g_hdiff || -drg > g_hdiff) && xg > 0.0f) || ((-dtg > g_hdiff || -dbg > g_hdiff) && yg > 0.0f))
+        ng = (tg + lg + rg + ttg + bbg) / 5.0f;
+    tr = m * nr + (1.0f - m) * tr;
+    tg = m * ng + (1.0f - m) * tg;
 }
 
 }  // namespace hg

@@ -37,6 +37,20 @@ void launch_thermal_in(const StepConsts& c, const float* rock, const float4* tc,
 // smoothing pass on rock (run when c.smooth_m != 0)
 void launch_smooth(const StepConsts& c, const float* rock, float* rock_o, cudaStream_t st);
 
+// ---- two-layer per-pass kernels (hg_layers.cu) -----------------------------------
+void launch_flux2(const StepConsts& c, const float* rock, const float* dirt, const float* water, const float* fl,
+                  const float* fr, const float* ft, const float* fb, float* water_o, float* fl_o, float* fr_o,
+                  float* ft_o, float* fb_o, float* u, float* v, float* vz, cudaStream_t st);
+void launch_erosion2(const StepConsts& c, const float* u, const float* v, const float* vz, const float* rock,
+                     const float* dirt, float* rock_o, float* dirt_o, float* s0, float* s1, cudaStream_t st);
+void launch_sediment2(const StepConsts& c, const float* u, const float* v, const float* s0, const float* s1,
+                      float* s0_o, float* s1_o, float* water, cudaStream_t st);
+// thermal_erosion for layer 1 (dirt); thermal_transport reuses launch_thermal_in on the dirt field
+void launch_thermal_out1(const StepConsts& c, const float* rock, const float* dirt, float4* tc, float4* td,
+                         cudaStream_t st);
+void launch_smooth2(const StepConsts& c, const float* rock, const float* dirt, float* rock_o, float* dirt_o,
+                    cudaStream_t st);
+
 // ---- fused step (hg_fused.cu) ---------------------------------------------------
 // Rain settings without the step number (the kernels add the step).
 struct RainBase {

@@ -87,6 +87,8 @@ struct hg_world {
     float4* td = nullptr;
     float* ks = nullptr;
     bool ks_on = false;
+    float* dirt[2] = {};      // two-layer worlds: dirt (current, alternate)
+    float* sdirt[2] = {};     // two-layer worlds: dirt sediment (current, alternate)
     float* s_ero = nullptr;  // fused step: eroded sediment of every cell
     float* b_ero = nullptr;  // fused step: eroded rock of every cell
     int* err = nullptr;      // device flag: a bounded wait gave up
@@ -188,6 +190,10 @@ void free_world(hg_world* w) {
     cudaFree(w->u); cudaFree(w->v); cudaFree(w->vz);
     cudaFree(w->tc); cudaFree(w->td);
     cudaFree(w->ks);
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(w->dirt[k]);
+        cudaFree(w->sdirt[k]);
+    }
     cudaFree(w->s_ero); cudaFree(w->b_ero); cudaFree(w->err); cudaFree(w->d_step);
     for (Plan*& p : w->plans) destroy_plan(p);
     cudaFree(w->red_f); cudaFree(w->red_d);
@@ -242,7 +248,7 @@ bool thermal_on(const hg_world* w) {
 
 StepConsts make_consts(const hg_world* w);
 // the reversed step covers rain, flux, erosion and sediment transport
-bool adjoint_covers(const hg_world* w) { return make_consts(w).smooth_m == 0.0f; }
+bool adjoint_covers(const hg_world* w) { return w->layers == 1 && make_consts(w).smooth_m == 0.0f; }
 
 StepConsts make_consts(const hg_world* w) {
     StepConsts c{};
@@ -276,6 +282,10 @@ StepConsts make_consts(const hg_world* w) {
     volatile float k1dt = s.Kspeed[1] * dt;
     float m = k1dt < 0.0f ? 0.0f : (float)k1dt;
     c.smooth_m = 1.0f < m ? 1.0f : m;
+    c.Ks1 = s.Ks[1];
+    c.Kconv = s.Kconv;
+    c.Kalpha1 = s.Kalpha[1];
+    c.Kspeed1 = s.Kspeed[1];
     return c;
 }
 
@@ -480,8 +490,10 @@ int run_plan(Plan* p, int nsteps, bool use_graph) {
 // variant gives identical fields, so tuning steps are ordinary steps.
 int fused_run(Plan** plans, const std::vector<hg_world*>& worlds, Tuning& tune, int req_th, int req_graph,
               cudaStream_t st, int* err, int nsteps) {
-    for (hg_world* w : worlds)
+    for (hg_world* w : worlds) {
         if (!fused_tile_ok(w->n, 16)) return fail(HG_ERR_UNSUPPORTED, "fused mode needs n divisible by 64");
+        if (w->layers != 1) return fail(HG_ERR_UNSUPPORTED, "the fused step covers one-layer worlds");
+    }
     if (req_th != HG_AUTO && req_th != 16 && req_th != 8)
         return fail(HG_ERR_UNSUPPORTED, "fused tile height must be 16 or 8");
     auto plan_for = [&](int th) -> Plan* {
@@ -537,6 +549,8 @@ float* field_ptr(hg_world* w, int field) {
         case HG_FIELD_VEL_V: return w->v;
         case HG_FIELD_VEL_Z: return w->vz;
         case HG_FIELD_KS: return w->ks;
+        case HG_FIELD_DIRT: return w->dirt[0];
+        case HG_FIELD_SEDIMENT_DIRT: return w->sdirt[0];
     }
     return nullptr;
 }
@@ -594,15 +608,17 @@ int hg_world_create(int n, int layers, hg_world** out) {
     if (!out) return fail(HG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (n <= 0 || n % 8 != 0) return fail(HG_ERR_INVALID, "n must be a positive multiple of 8");
-    if (layers != 1) return fail(HG_ERR_UNSUPPORTED, "only the one-layer (rock) world is supported");
+    if (layers != 1 && layers != 2) return fail(HG_ERR_UNSUPPORTED, "layers must be 1 or 2");
     hg_world* w = new (std::nothrow) hg_world();
     if (!w) return fail(HG_ERR_OOM, "host allocation failed");
     w->n = n;
     w->layers = layers;
     cudaGetDevice(&w->device);
     hg_default_erosion_settings(&w->es);
-    w->es.Kconv = 0.0f;       // one-layer world: no dirt layer to convert into
-    w->es.Kspeed[1] = 0.0f;
+    if (layers == 1) {
+        w->es.Kconv = 0.0f;       // one-layer world: no dirt layer to convert into
+        w->es.Kspeed[1] = 0.0f;
+    }
     hg_default_rain_settings(&w->rs);
     hg_default_step_options(&w->opt);
     size_t bytes = (size_t)n * n * sizeof(float);
@@ -618,6 +634,12 @@ int hg_world_create(int n, int layers, hg_world** out) {
     if (e == cudaSuccess) e = alloc((void**)&w->tc, 4 * bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->td, 4 * bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->ks, bytes);
+    for (int k = 0; k < 2 && layers == 2 && e == cudaSuccess; ++k) {
+        e = alloc((void**)&w->dirt[k], bytes);
+        if (e == cudaSuccess) e = alloc((void**)&w->sdirt[k], bytes);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w->dirt[k], 0, bytes, w->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(w->sdirt[k], 0, bytes, w->stream);
+    }
     if (e == cudaSuccess) e = alloc((void**)&w->s_ero, bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->b_ero, bytes);
     if (e == cudaSuccess) e = alloc((void**)&w->err, sizeof(int));
@@ -832,7 +854,45 @@ int hg_step(hg_world* w, int nsteps, int mode) {
     StepConsts c = make_consts(w);
     cudaStream_t st = w->stream;
     auto swap = [&](int f) { float* t = w->cur[f]; w->cur[f] = w->alt[f]; w->alt[f] = t; };
-    if (mode == HG_MODE_PLAIN) {
+    if (mode == HG_MODE_PLAIN && w->layers == 2) {
+        // the reference's two-layer step (src/erosion.cpp:158-200): thermal
+        // and smoothing passes for layers whose slippage rate is 0 are
+        // identities and are skipped
+        auto swap2 = [](float** f) { float* t = f[0]; f[0] = f[1]; f[1] = t; };
+        for (int k = 0; k < nsteps; ++k) {
+            RainStep r = make_rain(w, w->step + 1);
+            if (r.active) launch_rain(c, r, w->cur[S_WATER], st);
+            launch_flux2(c, w->cur[S_ROCK], w->dirt[0], w->cur[S_WATER], w->cur[S_FL], w->cur[S_FR], w->cur[S_FT],
+                         w->cur[S_FB], w->alt[S_WATER], w->alt[S_FL], w->alt[S_FR], w->alt[S_FT], w->alt[S_FB],
+                         w->u, w->v, w->vz, st);
+            swap(S_WATER); swap(S_FL); swap(S_FR); swap(S_FT); swap(S_FB);
+            launch_erosion2(c, w->u, w->v, w->vz, w->cur[S_ROCK], w->dirt[0], w->alt[S_ROCK], w->dirt[1],
+                            w->cur[S_SED], w->sdirt[0], st);
+            swap(S_ROCK);
+            swap2(w->dirt);
+            launch_sediment2(c, w->u, w->v, w->cur[S_SED], w->sdirt[0], w->alt[S_SED], w->sdirt[1], w->cur[S_WATER],
+                             st);
+            swap(S_SED);
+            swap2(w->sdirt);
+            if (c.thermal) {  // layer 0: drops of rock only
+                launch_thermal_out(c, w->cur[S_ROCK], w->tc, w->td, st);
+                launch_thermal_in(c, w->cur[S_ROCK], w->tc, w->td, w->alt[S_ROCK], st);
+                swap(S_ROCK);
+            }
+            if (c.Kspeed1 != 0.0f) {  // layer 1: drops of rock + dirt, dirt moves
+                launch_thermal_out1(c, w->cur[S_ROCK], w->dirt[0], w->tc, w->td, st);
+                launch_thermal_in(c, w->dirt[0], w->tc, w->td, w->dirt[1], st);
+                swap2(w->dirt);
+            }
+            if (c.smooth_m != 0.0f) {
+                launch_smooth2(c, w->cur[S_ROCK], w->dirt[0], w->alt[S_ROCK], w->dirt[1], st);
+                swap(S_ROCK);
+                swap2(w->dirt);
+            }
+            w->step += 1;
+        }
+        if (nsteps > 0) w->dev_step_valid = false;
+    } else if (mode == HG_MODE_PLAIN) {
         for (int k = 0; k < nsteps; ++k) {
             RainStep r = make_rain(w, w->step + 1);
             if (r.active) launch_rain(c, r, w->cur[S_WATER], st);
@@ -859,6 +919,7 @@ int hg_step(hg_world* w, int nsteps, int mode) {
         }
         if (nsteps > 0) w->dev_step_valid = false;
     } else if (nsteps > 0) {
+        if (w->layers != 1) return fail(HG_ERR_UNSUPPORTED, "the fused step covers one-layer worlds");
         std::vector<hg_world*> one{w};
         int rc = fused_run(w->plans, one, w->tuning, w->opt.tile_y, w->opt.graph, st, w->err, nsteps);
         if (rc != HG_OK) return rc;
@@ -1115,7 +1176,7 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     if (!out) return fail(HG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (nsteps < 1) return fail(HG_ERR_INVALID, "nsteps must be >= 1");
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without smoothing (Kspeed[1] == 0)");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0)");
     if (!fused_tile_ok(w->n, 16) || !adjoint_tile_ok(w->n))
         return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
     DeviceGuard g(w->device);
@@ -1237,7 +1298,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
 int hg_forward(hg_tape* t) {
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     hg_world* w = t->w;
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without smoothing (Kspeed[1] == 0)");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0)");
     DeviceGuard g(w->device);
     t->step0 = w->step;
     const size_t c = cells(w);
@@ -1272,7 +1333,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
     if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
     hg_world* w = t->w;
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers the step without smoothing (Kspeed[1] == 0)");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0)");
     DeviceGuard g(w->device);
     cudaStream_t st = w->stream;
     const size_t c = cells(w), sf = kStateFields * c;
@@ -1427,8 +1488,18 @@ struct CkptHeader {
     hg_step_options opt;
 };
 const char kCkptMagic[8] = {'H', 'G', 'W', 'O', 'R', 'L', 'D', '1'};
-const int kCkptFields[] = {HG_FIELD_ROCK,   HG_FIELD_WATER,  HG_FIELD_SEDIMENT, HG_FIELD_FLUX_L, HG_FIELD_FLUX_R,
-                           HG_FIELD_FLUX_T, HG_FIELD_FLUX_B, HG_FIELD_VEL_U,    HG_FIELD_VEL_V};
+// the nine carried fields, then dirt and dirt sediment (two-layer worlds),
+// then the per-cell Ks field when set
+std::vector<int> ckpt_fields(int layers, bool ks_on) {
+    std::vector<int> f = {HG_FIELD_ROCK,   HG_FIELD_WATER,  HG_FIELD_SEDIMENT, HG_FIELD_FLUX_L, HG_FIELD_FLUX_R,
+                          HG_FIELD_FLUX_T, HG_FIELD_FLUX_B, HG_FIELD_VEL_U,    HG_FIELD_VEL_V};
+    if (layers == 2) {
+        f.push_back(HG_FIELD_DIRT);
+        f.push_back(HG_FIELD_SEDIMENT_DIRT);
+    }
+    if (ks_on) f.push_back(HG_FIELD_KS);
+    return f;
+}
 }  // namespace
 
 int hg_world_save(hg_world* w, const char* path) {
@@ -1440,7 +1511,8 @@ int hg_world_save(hg_world* w, const char* path) {
     h.version = 1;
     h.n = w->n;
     h.layers = w->layers;
-    h.nfields = 9 + (w->ks_on ? 1 : 0);
+    const std::vector<int> fields = ckpt_fields(w->layers, w->ks_on);
+    h.nfields = (uint32_t)fields.size();
     h.step = w->step;
     h.es = w->es;
     h.rs = w->rs;
@@ -1452,8 +1524,8 @@ int hg_world_save(hg_world* w, const char* path) {
     bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
     HG_CUDA(cudaStreamSynchronize(w->stream));
     for (uint32_t k = 0; ok && k < h.nfields; ++k) {
-        int field = k < 9 ? kCkptFields[k] : HG_FIELD_KS;
-        cudaError_t e = cudaMemcpy(buf.data(), field_ptr(w, field), buf.size() * sizeof(float), cudaMemcpyDeviceToHost);
+        cudaError_t e =
+            cudaMemcpy(buf.data(), field_ptr(w, fields[k]), buf.size() * sizeof(float), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) {
             std::fclose(f);
             return cuda_fail(e, "checkpoint download");
@@ -1476,13 +1548,18 @@ int hg_world_load(hg_world* w, const char* path) {
         std::fclose(f);
         return fail(HG_ERR_IO, std::string("not a world checkpoint: ") + path);
     }
-    if (h.n != w->n || h.layers != w->layers || h.nfields < 9 || h.nfields > 10) {
+    if (h.n != w->n || h.layers != w->layers) {
         std::fclose(f);
         return fail(HG_ERR_INVALID, "checkpoint world size or layer count differs from this world");
     }
+    const std::vector<int> fields = ckpt_fields(h.layers, h.ks_on != 0);
+    if (h.nfields != fields.size()) {
+        std::fclose(f);
+        return fail(HG_ERR_IO, std::string("inconsistent checkpoint header: ") + path);
+    }
     std::vector<float> buf(cells(w));
     for (uint32_t k = 0; k < h.nfields; ++k) {
-        int field = k < 9 ? kCkptFields[k] : HG_FIELD_KS;
+        int field = fields[k];
         if (std::fread(buf.data(), sizeof(float), buf.size(), f) != buf.size()) {
             std::fclose(f);
             return fail(HG_ERR_IO, std::string("truncated checkpoint: ") + path);

@@ -28,7 +28,7 @@ HG_AUTO = -1
 RAIN_OFF, RAIN_UNIFORM, RAIN_BERNOULLI = 0, 1, 2
 MODE_PLAIN, MODE_FUSED, MODE_FUSED_PER_WORLD = 0, 1, 2
 FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_t": 5, "flux_b": 6,
-          "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10}
+          "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10, "dirt": 11, "sediment_dirt": 12}
 STATE_FIELDS = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"]
 
 

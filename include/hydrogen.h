@@ -124,7 +124,9 @@ typedef struct hg_noise_settings {
 #define HG_FIELD_VEL_V 8     /* velocitymap.y */
 #define HG_FIELD_VEL_Z 9     /* velocitymap.z = d1+d2 of the last plain step */
 #define HG_FIELD_KS 10       /* per-cell rock solubility (replaces Ks[0]) */
-#define HG_FIELD_COUNT 11
+#define HG_FIELD_DIRT 11     /* heightmap.g: dirt layer (two-layer worlds) */
+#define HG_FIELD_SEDIMENT_DIRT 12 /* sedimap.g: suspended dirt (two-layer worlds) */
+#define HG_FIELD_COUNT 13
 
 #define HG_MODE_PLAIN 0           /* one kernel per GLSL pass */
 #define HG_MODE_FUSED 1           /* two fused, tiled kernels per step */
@@ -148,8 +150,13 @@ int hg_default_step_options(hg_step_options* out);
 /* ---- world ------------------------------------------------------------------------- */
 /* Replaces State::World::gen_textures (src/state.cpp:3-44): allocates the
  * device fields of an n x n world (n a positive multiple of 8,
- * src/erosion.cpp:83-84) on the current device.  layers must be 1 (rock with
- * an empty dirt layer).  All fields start at zero. */
+ * src/erosion.cpp:83-84) on the current device.  layers 1: rock with an
+ * empty dirt layer (Kconv and the dirt layer's terms vanish; every mode);
+ * layers 2: the reference's rock + dirt model with both sediment channels
+ * (HG_MODE_PLAIN only; fused steps, batches in fused mode and tapes need
+ * layers 1).  All fields start at zero; the settings start at the
+ * reference's defaults (src/state.cpp:81-92), with Kconv and Kspeed[1] at 0
+ * for one-layer worlds. */
 int hg_world_create(int n, int layers, hg_world** out);
 /* Replaces State::World::delete_textures (src/state.cpp:46-55). */
 int hg_world_destroy(hg_world* w);

@@ -62,7 +62,7 @@ def test_error_paths_without_a_device(hg):
     h = ctypes.c_void_p()
     assert hg.lib.hg_world_create(12, 1, ctypes.byref(h)) == -1  # not a multiple of 8
     assert b"multiple of 8" in hg.lib.hg_last_error()
-    assert hg.lib.hg_world_create(64, 2, ctypes.byref(h)) == -5
+    assert hg.lib.hg_world_create(64, 3, ctypes.byref(h)) == -5  # layers 1 (rock) or 2 (rock + dirt)
     assert hg.lib.hg_step(None, 1, 0) == -1
     assert hg.lib.hg_world_destroy(None) == 0
 
