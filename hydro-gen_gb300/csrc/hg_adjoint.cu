@@ -45,10 +45,10 @@ __device__ __forceinline__ size_t at(int n, int x, int y) { return (size_t)y * n
 // Cell (x, y) of a step whose output sediment adjoint is `a`: scatter to the
 // back-trace taps of dse, back-trace velocity adjoint into du, dv.
 __device__ __forceinline__ void sediment_adjoint(const StepConsts& c, const AdjSlot& sl, int x, int y, size_t i,
-                                                 float a, float* dse, float* du, float* dv) {
+                                                 float a, float ui, float vi, float* dse, float* du, float* dv) {
     const int n = c.n;
     const float maxc = (float)(n - 1);
-    float rx = (float)x - sl.u[i] * c.dt, ry = (float)y - sl.v[i] * c.dt;
+    float rx = (float)x - ui * c.dt, ry = (float)y - vi * c.dt;
     float px = gclamp(rx, 0.0f, maxc), py = gclamp(ry, 0.0f, maxc);
     int ix = min(max((int)px, 0), n - 1), iy = min(max((int)py, 0), n - 1);
     float fx = px - floorf(px), fy = py - floorf(py);
@@ -73,7 +73,7 @@ __global__ void k_adj_sediment(StepConsts c, AdjSlot sl, const float* __restrict
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= c.n || y >= c.n) return;
     size_t i = at(c.n, x, y);
-    sediment_adjoint(c, sl, x, y, i, as_[i], dse, du, dv);
+    sediment_adjoint(c, sl, x, y, i, as_[i], sl.u[i], sl.v[i], dse, du, dv);
 }
 
 // Gathered adjoint of a state at cell i: own terms plus the neighbours'
@@ -188,6 +188,8 @@ __device__ __forceinline__ void adj_tile(const AdjCellArgs& a, float* sm, uint64
     const float as = a.dse[i];
     const float DUs = a.du[i], DVs = a.dv[i];
     const float Ks_i = c.ks_field ? c.ks_field[i] : c.Ks0;
+    // step j - 1's velocity for its sediment reversal at the end
+    const float pu = a.scatter_prev ? a.prev.u[i] : 0.0f, pv = a.scatter_prev ? a.prev.v[i] : 0.0f;
     bool ok = __syncthreads_and(mbar_wait(bar, 0));
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
@@ -344,7 +346,7 @@ __device__ __forceinline__ void adj_tile(const AdjCellArgs& a, float* sm, uint64
         a.rd[i] = gw + gd1;
         a.rs[i] = gs;
         // ---- sediment_transport of step j - 1 reversed ----------------------
-        if (a.scatter_prev) sediment_adjoint(c, a.prev, x, y, i, gs, a.dse_prev, a.du, a.dv);
+        if (a.scatter_prev) sediment_adjoint(c, a.prev, x, y, i, gs, pu, pv, a.dse_prev, a.du, a.dv);
     }
 }
 
