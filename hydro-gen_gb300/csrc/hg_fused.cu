@@ -86,7 +86,9 @@ __device__ __forceinline__ int find_terrain(const int* tile0, int nterr, int til
 
 __device__ __forceinline__ RainStep rain_for(const RainBase& rb, unsigned long long step1) {
     RainStep r;
-    r.active = (rb.mode != 0 && rb.period > 0 && step1 % (unsigned long long)rb.period == 0ull) ? 1 : 0;
+    // uniform and Bernoulli rain only: the reference rain runs as its own
+    // kernel before the step (the host inserts it)
+    r.active = ((rb.mode == 1 || rb.mode == 2) && rb.period > 0 && step1 % (unsigned long long)rb.period == 0ull) ? 1 : 0;
     r.bernoulli = rb.mode == 2 ? 1 : 0;
     r.amount = rb.amount;
     r.threshold = rb.threshold;

@@ -37,6 +37,12 @@ void launch_thermal_in(const StepConsts& c, const float* rock, const float4* tc,
 // smoothing pass on rock (run when c.smooth_m != 0)
 void launch_smooth(const StepConsts& c, const float* rock, float* rock_o, cudaStream_t st);
 
+// ---- the reference's terrain generator and rain (hg_terrain.cu) --------------------
+void launch_ref_heightmap(const hg_map_settings& cfg, int n, float* rock, float* dirt, cudaStream_t st);
+// water += the reference's rain at frame time `time`; dirt may be nullptr (one layer)
+void launch_ref_rain(const hg_rain_settings& rs, const hg_map_settings& map, float time, int n, const float* rock,
+                     const float* dirt, float* water, cudaStream_t st);
+
 // ---- two-layer per-pass kernels (hg_layers.cu) -----------------------------------
 void launch_flux2(const StepConsts& c, const float* rock, const float* dirt, const float* water, const float* fl,
                   const float* fr, const float* ft, const float* fb, float* water_o, float* fl_o, float* fr_o,

@@ -76,6 +76,7 @@ struct hg_world {
     cudaStream_t stream = nullptr;
     hg_erosion_settings es{};
     hg_rain_settings rs{};
+    hg_map_settings map{};
     hg_step_options opt{};
     uint64_t step = 0;
     float* cur[S_COUNT] = {};
@@ -248,7 +249,9 @@ bool thermal_on(const hg_world* w) {
 
 StepConsts make_consts(const hg_world* w);
 // the reversed step covers rain, flux, erosion and sediment transport
-bool adjoint_covers(const hg_world* w) { return w->layers == 1 && make_consts(w).smooth_m == 0.0f; }
+bool adjoint_covers(const hg_world* w) {
+    return w->layers == 1 && make_consts(w).smooth_m == 0.0f && w->opt.rain_mode != HG_RAIN_REFERENCE;
+}
 
 StepConsts make_consts(const hg_world* w) {
     StepConsts c{};
@@ -321,6 +324,22 @@ RainBase make_rain_base(const hg_world* w) {
 }
 
 __global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+
+// frame time of step step1 for the reference rain
+float rain_time(const hg_world* w, uint64_t step1) {
+    return (float)((double)w->opt.rain_time0 + (double)step1 * (double)w->opt.rain_time_step);
+}
+
+// The rain pass of step step1 (1-based) on `water`, if it rains then.
+void rain_pass(hg_world* w, const StepConsts& c, uint64_t step1, const float* rock, const float* dirt, float* water,
+               cudaStream_t st) {
+    RainStep r = make_rain(w, step1);
+    if (!r.active) return;
+    if (w->opt.rain_mode == HG_RAIN_REFERENCE)
+        launch_ref_rain(w->rs, w->map, rain_time(w, step1), w->n, rock, dirt, water, st);
+    else
+        launch_rain(c, r, water, st);
+}
 
 // Fills both descriptor tables of a plan from its worlds' current buffers
 // (table 0 steps cur -> alt, table 1 alt -> cur) and records the build state.
@@ -462,6 +481,11 @@ int prepare_plan(Plan* p, bool use_graph, int* dir_out) {
 
 // Runs nsteps fused steps of a plan's worlds on the plan's stream.
 int run_plan(Plan* p, int nsteps, bool use_graph) {
+    // the reference rain runs as its own kernel before the steps it falls on,
+    // so a plan with such a world launches step by step
+    bool ref_rain = false;
+    for (hg_world* w : p->worlds) ref_rain = ref_rain || w->opt.rain_mode == HG_RAIN_REFERENCE;
+    if (ref_rain) use_graph = false;
     int dir = 0;
     int rc = prepare_plan(p, use_graph && nsteps >= 2, &dir);
     if (rc != HG_OK) return rc;
@@ -473,8 +497,18 @@ int run_plan(Plan* p, int nsteps, bool use_graph) {
             count_launch(p->graph_launches);
         }
     }
-    for (; k < nsteps; ++k)
-        launch_dir(p, (dir + k) & 1);
+    for (; k < nsteps; ++k) {
+        const int d = (dir + k) & 1;
+        if (ref_rain)  // the step's input water: the buffers of direction d at the plan's build
+            for (int i = 0; i < nt; ++i) {
+                hg_world* w = p->worlds[i];
+                if (w->opt.rain_mode != HG_RAIN_REFERENCE) continue;
+                const auto& in = d == 0 ? p->key_cur[i] : p->key_alt[i];
+                rain_pass(w, StepConsts{}, w->step + (uint64_t)k + 1, in[S_ROCK], nullptr,
+                          const_cast<float*>(in[S_WATER]), p->stream);
+            }
+        launch_dir(p, d);
+    }
     HG_CUDA(cudaGetLastError());
     for (hg_world* w : p->worlds) {
         w->step += (uint64_t)nsteps;
@@ -620,6 +654,7 @@ int hg_world_create(int n, int layers, hg_world** out) {
         w->es.Kspeed[1] = 0.0f;
     }
     hg_default_rain_settings(&w->rs);
+    hg_default_map_settings(&w->map);
     hg_default_step_options(&w->opt);
     size_t bytes = (size_t)n * n * sizeof(float);
     auto alloc = [&](void** p, size_t b) -> cudaError_t { return cudaMalloc(p, b); };
@@ -725,7 +760,7 @@ int hg_set_rain_settings(hg_world* w, const hg_rain_settings* s) {
 int hg_set_step_options(hg_world* w, const hg_step_options* o) {
     HG_CHECK_WORLD(w);
     if (!o) return fail(HG_ERR_INVALID, "null options");
-    if (o->rain_mode < HG_RAIN_OFF || o->rain_mode > HG_RAIN_BERNOULLI) return fail(HG_ERR_INVALID, "bad rain_mode");
+    if (o->rain_mode < HG_RAIN_OFF || o->rain_mode > HG_RAIN_REFERENCE) return fail(HG_ERR_INVALID, "bad rain_mode");
     if (!(o->rain_probability >= 0.0f && o->rain_probability <= 1.0f))
         return fail(HG_ERR_INVALID, "rain_probability must be in [0, 1]");
     if (o->tile_x != HG_AUTO && o->tile_x != 64) return fail(HG_ERR_UNSUPPORTED, "fused tile width must be 64");
@@ -737,11 +772,9 @@ int hg_set_step_options(hg_world* w, const hg_step_options* o) {
     return HG_OK;
 }
 
-int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
-    HG_CHECK_WORLD(w);
-    if (!s) return fail(HG_ERR_INVALID, "null noise settings");
-    if (s->octaves < 1 || s->octaves > 32) return fail(HG_ERR_INVALID, "octaves must be in [1, 32]");
-    DeviceGuard g(w->device);
+namespace {
+// every state field (and the dirt layer's) back to zero
+int zero_state(hg_world* w) {
     size_t bytes = cells(w) * sizeof(float);
     for (int f = 0; f < S_COUNT; ++f) {
         HG_CUDA(cudaMemsetAsync(w->cur[f], 0, bytes, w->stream));
@@ -750,6 +783,76 @@ int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
     HG_CUDA(cudaMemsetAsync(w->u, 0, bytes, w->stream));
     HG_CUDA(cudaMemsetAsync(w->v, 0, bytes, w->stream));
     HG_CUDA(cudaMemsetAsync(w->vz, 0, bytes, w->stream));
+    for (int k = 0; k < 2 && w->layers == 2; ++k) {
+        HG_CUDA(cudaMemsetAsync(w->dirt[k], 0, bytes, w->stream));
+        HG_CUDA(cudaMemsetAsync(w->sdirt[k], 0, bytes, w->stream));
+    }
+    return HG_OK;
+}
+
+int check_map_settings(const hg_map_settings* s) {
+    if (!s) return fail(HG_ERR_INVALID, "null map settings");
+    if (s->octaves < 0) return fail(HG_ERR_INVALID, "octaves must be >= 0");
+    if (!(s->max_height > 0.0f)) return fail(HG_ERR_INVALID, "max_height must be positive");
+    return HG_OK;
+}
+}  // namespace
+
+int hg_default_map_settings(hg_map_settings* out) {
+    if (!out) return fail(HG_ERR_INVALID, "null settings");
+    std::memset(out, 0, sizeof(*out));
+    // src/settings.hpp:27-57 (MAX_HEIGHT 256, WATER_HEIGHT 96)
+    out->max_height = 256.0f;
+    out->max_dirt = 2.0f;
+    out->hmap_dims[0] = out->hmap_dims[1] = 1024;
+    out->height_mult = 1.0f;
+    out->water_lvl = 96.0f;
+    out->seed = 0.0f;
+    out->persistance = 0.44f;
+    out->lacunarity = 2.0f;
+    out->scale = 0.00075f;
+    out->redistribution = 1.0f;
+    out->octaves = 8;
+    out->mask_exp = 1;
+    out->mask_power = 1;
+    out->uplift_scale = 1.16f;
+    out->domain_warp = 1;
+    out->domain_warp_scale = 100.0f;
+    out->terrace_scale = 0.5f;
+    return HG_OK;
+}
+
+int hg_set_map_settings(hg_world* w, const hg_map_settings* s) {
+    HG_CHECK_WORLD(w);
+    int rc = check_map_settings(s);
+    if (rc != HG_OK) return rc;
+    w->map = *s;
+    w->version += 1;
+    return HG_OK;
+}
+
+int hg_init_reference_heightmap(hg_world* w, const hg_map_settings* s) {
+    HG_CHECK_WORLD(w);
+    int rc = check_map_settings(s);
+    if (rc != HG_OK) return rc;
+    DeviceGuard g(w->device);
+    if ((rc = zero_state(w)) != HG_OK) return rc;
+    launch_ref_heightmap(*s, w->n, w->cur[S_ROCK], w->layers == 2 ? w->dirt[0] : nullptr, w->stream);
+    HG_CUDA(cudaGetLastError());
+    w->map = *s;
+    w->version += 1;
+    w->step = 0;
+    w->dev_step_valid = false;
+    return HG_OK;
+}
+
+int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
+    HG_CHECK_WORLD(w);
+    if (!s) return fail(HG_ERR_INVALID, "null noise settings");
+    if (s->octaves < 1 || s->octaves > 32) return fail(HG_ERR_INVALID, "octaves must be in [1, 32]");
+    DeviceGuard g(w->device);
+    int zrc = zero_state(w);
+    if (zrc != HG_OK) return zrc;
     launch_fbm_raw(w->cur[S_ROCK], w->n, *s, w->stream);
     launch_minmax(w->cur[S_ROCK], cells(w), w->red_f, reduction_parts(), w->red_f + 2 * reduction_parts(),
                   w->stream);
@@ -860,8 +963,7 @@ int hg_step(hg_world* w, int nsteps, int mode) {
         // identities and are skipped
         auto swap2 = [](float** f) { float* t = f[0]; f[0] = f[1]; f[1] = t; };
         for (int k = 0; k < nsteps; ++k) {
-            RainStep r = make_rain(w, w->step + 1);
-            if (r.active) launch_rain(c, r, w->cur[S_WATER], st);
+            rain_pass(w, c, w->step + 1, w->cur[S_ROCK], w->dirt[0], w->cur[S_WATER], st);
             launch_flux2(c, w->cur[S_ROCK], w->dirt[0], w->cur[S_WATER], w->cur[S_FL], w->cur[S_FR], w->cur[S_FT],
                          w->cur[S_FB], w->alt[S_WATER], w->alt[S_FL], w->alt[S_FR], w->alt[S_FT], w->alt[S_FB],
                          w->u, w->v, w->vz, st);
@@ -894,8 +996,7 @@ int hg_step(hg_world* w, int nsteps, int mode) {
         if (nsteps > 0) w->dev_step_valid = false;
     } else if (mode == HG_MODE_PLAIN) {
         for (int k = 0; k < nsteps; ++k) {
-            RainStep r = make_rain(w, w->step + 1);
-            if (r.active) launch_rain(c, r, w->cur[S_WATER], st);
+            rain_pass(w, c, w->step + 1, w->cur[S_ROCK], nullptr, w->cur[S_WATER], st);
             launch_flux(c, w->cur[S_ROCK], w->cur[S_WATER], w->cur[S_FL], w->cur[S_FR], w->cur[S_FT],
                         w->cur[S_FB], w->alt[S_WATER], w->alt[S_FL], w->alt[S_FR], w->alt[S_FT], w->alt[S_FB],
                         w->u, w->v, w->vz, st);
@@ -1176,7 +1277,7 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     if (!out) return fail(HG_ERR_INVALID, "null output pointer");
     *out = nullptr;
     if (nsteps < 1) return fail(HG_ERR_INVALID, "nsteps must be >= 1");
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0)");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0) or the reference rain");
     if (!fused_tile_ok(w->n, 16) || !adjoint_tile_ok(w->n))
         return fail(HG_ERR_UNSUPPORTED, "the adjoint needs n divisible by 64");
     DeviceGuard g(w->device);
@@ -1298,7 +1399,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
 int hg_forward(hg_tape* t) {
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     hg_world* w = t->w;
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0)");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0) or the reference rain");
     DeviceGuard g(w->device);
     t->step0 = w->step;
     const size_t c = cells(w);
@@ -1333,7 +1434,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
     if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
     hg_world* w = t->w;
-    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0)");
+    if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0) or the reference rain");
     DeviceGuard g(w->device);
     cudaStream_t st = w->stream;
     const size_t c = cells(w), sf = kStateFields * c;

@@ -25,7 +25,7 @@ HG_OK = 0
 STATUS = {-1: "HG_ERR_INVALID", -2: "HG_ERR_OOM", -3: "HG_ERR_CUDA", -4: "HG_ERR_TIMEOUT",
           -5: "HG_ERR_UNSUPPORTED", -6: "HG_ERR_IO", -7: "HG_ERR_STATE"}
 HG_AUTO = -1
-RAIN_OFF, RAIN_UNIFORM, RAIN_BERNOULLI = 0, 1, 2
+RAIN_OFF, RAIN_UNIFORM, RAIN_BERNOULLI, RAIN_REFERENCE = 0, 1, 2, 3
 MODE_PLAIN, MODE_FUSED, MODE_FUSED_PER_WORLD = 0, 1, 2
 FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_t": 5, "flux_b": 6,
           "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10, "dirt": 11, "sediment_dirt": 12}
@@ -59,7 +59,19 @@ class StepOptions(ctypes.Structure):
     _fields_ = [("rain_mode", ctypes.c_int32), ("rain_probability", ctypes.c_float),
                 ("rain_seed", ctypes.c_uint64), ("terrain_id", ctypes.c_uint32), ("thermal", ctypes.c_int32),
                 ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32), ("graph", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("rain_time0", ctypes.c_float), ("rain_time_step", ctypes.c_float), ("reserved", ctypes.c_int32 * 4)]
+
+
+class MapSettings(ctypes.Structure):
+    """Map_settings_data, glsl/bindings.glsl:70-99 (std140, 96 bytes)."""
+    _fields_ = [("max_height", ctypes.c_float), ("max_dirt", ctypes.c_float), ("hmap_dims", ctypes.c_int32 * 2),
+                ("height_mult", ctypes.c_float), ("water_lvl", ctypes.c_float), ("seed", ctypes.c_float),
+                ("persistance", ctypes.c_float), ("lacunarity", ctypes.c_float), ("scale", ctypes.c_float),
+                ("redistribution", ctypes.c_float), ("octaves", ctypes.c_int32), ("fake_erosion", ctypes.c_uint32),
+                ("mask_round", ctypes.c_uint32), ("mask_exp", ctypes.c_uint32), ("mask_power", ctypes.c_uint32),
+                ("mask_slope", ctypes.c_uint32), ("uplift", ctypes.c_uint32), ("uplift_scale", ctypes.c_float),
+                ("domain_warp", ctypes.c_int32), ("domain_warp_scale", ctypes.c_float), ("terrace", ctypes.c_int32),
+                ("terrace_scale", ctypes.c_float), ("pad0", ctypes.c_float)]
 
 
 class NoiseSettings(ctypes.Structure):
@@ -108,6 +120,9 @@ def _load():
         "hg_batch_step": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
         "hg_batch_sync": (ctypes.c_int, [P]),
         "hg_batch_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
+        "hg_default_map_settings": (ctypes.c_int, [ctypes.POINTER(MapSettings)]),
+        "hg_set_map_settings": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
+        "hg_init_reference_heightmap": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
         "hg_selftest_division": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
         "hg_batch_launch_form": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
         "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
@@ -182,7 +197,7 @@ def rain_uniform(amount=0.01, period=1):
 
 
 def options(rain_mode=RAIN_UNIFORM, p=0.0, seed=0, terrain_id=0, thermal=HG_AUTO, tile=(HG_AUTO, HG_AUTO),
-            graph=HG_AUTO):
+            graph=HG_AUTO, time0=0.0, time_step=0.0):
     o = StepOptions()
     check(lib.hg_default_step_options(ctypes.byref(o)))
     o.rain_mode = rain_mode
@@ -192,7 +207,18 @@ def options(rain_mode=RAIN_UNIFORM, p=0.0, seed=0, terrain_id=0, thermal=HG_AUTO
     o.thermal = thermal
     o.tile_x, o.tile_y = tile
     o.graph = graph
+    o.rain_time0 = time0
+    o.rain_time_step = time_step
     return o
+
+
+def map_settings(**kw):
+    """The reference's map defaults (seed 0) with fields overridden by keyword."""
+    m = MapSettings()
+    check(lib.hg_default_map_settings(ctypes.byref(m)))
+    for k, v in kw.items():
+        setattr(m, k, v)
+    return m
 
 
 def noise(seed=0, octaves=6, frequency=1.0 / 128, lacunarity=2.0, gain=0.5, lo=0.0, hi=64.0):
@@ -246,6 +272,13 @@ class World:
 
     def init_heightmap(self, ns):
         check(lib.hg_init_heightmap(self.h, ctypes.byref(ns)))
+
+    def init_reference_heightmap(self, ms):
+        """The reference's terrain generator (glsl/heightmap.glsl)."""
+        check(lib.hg_init_reference_heightmap(self.h, ctypes.byref(ms)))
+
+    def set_map(self, ms):
+        check(lib.hg_set_map_settings(self.h, ctypes.byref(ms)))
 
     def init_ks_field(self, ns, base, k):
         check(lib.hg_init_ks_field(self.h, ctypes.byref(ns), base, k))

@@ -79,6 +79,10 @@ typedef struct hg_rain_settings {
 
 #define HG_RAIN_OFF 0       /* no rain pass */
 #define HG_RAIN_UNIFORM 1   /* every cell gains `amount` */
+#define HG_RAIN_REFERENCE 3 /* the reference's rain (glsl/rain.glsl:32-56): amount *
+                               max(0, simplex fBm) seeded by the frame time, plus
+                               the mountain bonus above mountain_thresh of the map's
+                               max_height (hg_set_map_settings) */
 #define HG_RAIN_BERNOULLI 2 /* a cell gains `amount` with probability p, drawn
                                from Philox4x32-10 keyed (seed, step, cell) */
 
@@ -96,8 +100,38 @@ typedef struct hg_step_options {
     int32_t tile_y;           /* fused mode tile height: HG_AUTO (autotuned), 16 or 8 */
     int32_t graph;            /* fused mode: replay a captured 2-step CUDA graph;
                                  HG_AUTO (autotuned), 0 or 1 */
-    int32_t reserved[6];
+    float rain_time0;         /* HG_RAIN_REFERENCE: the frame time of step k (1-based) */
+    float rain_time_step;     /*   is rain_time0 + k * rain_time_step (seconds) */
+    int32_t reserved[4];
 } hg_step_options;
+
+/* Map_settings_data (glsl/bindings.glsl:70-99): the reference's terrain
+ * generator settings, std140 layout (96 bytes). */
+typedef struct hg_map_settings {
+    float max_height;
+    float max_dirt;
+    int32_t hmap_dims[2];
+    float height_mult;
+    float water_lvl;
+    float seed;
+    float persistance;
+    float lacunarity;
+    float scale;
+    float redistribution;
+    int32_t octaves;
+    uint32_t fake_erosion;
+    uint32_t mask_round;
+    uint32_t mask_exp;
+    uint32_t mask_power;
+    uint32_t mask_slope;
+    uint32_t uplift;
+    float uplift_scale;
+    int32_t domain_warp;
+    float domain_warp_scale;
+    int32_t terrace;
+    float terrace_scale;
+    float _pad0;
+} hg_map_settings;
 
 /* Simplex fBm heightmap: octave o samples 2-D simplex noise at cell
  * coordinates times frequency*lacunarity^o with amplitude gain^o and hash
@@ -158,6 +192,21 @@ int hg_default_step_options(hg_step_options* out);
  * reference's defaults (src/state.cpp:81-92), with Kconv and Kspeed[1] at 0
  * for one-layer worlds. */
 int hg_world_create(int n, int layers, hg_world** out);
+
+/* The reference's map defaults (src/settings.hpp:27-57) with seed 0 (the
+ * reference draws it from rand()). */
+int hg_default_map_settings(hg_map_settings* out);
+/* Map settings of a world (the rain's mountain bonus reads max_height);
+ * "Set Map settings" equivalent. */
+int hg_set_map_settings(hg_world* w, const hg_map_settings* s);
+/* The reference's terrain generator (glsl/heightmap.glsl:52-158, called by
+ * World::gen_heightmap, src/state.cpp:116-147): derivative-damped gradient-
+ * noise fBm with domain warp, optional uplift, round/exponential/power/slope
+ * masks and terraces; rock = min(max_height, v * max_height * multiplier),
+ * dirt = (fBm + 1.5) * max_dirt in two-layer worlds.  Stores the map
+ * settings, zeroes water, sediment, flux and velocity, resets the step
+ * counter. */
+int hg_init_reference_heightmap(hg_world* w, const hg_map_settings* s);
 /* Replaces State::World::delete_textures (src/state.cpp:46-55). */
 int hg_world_destroy(hg_world* w);
 int hg_world_size(const hg_world* w, int* n);

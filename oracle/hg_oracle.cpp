@@ -84,7 +84,14 @@ struct OracleOptions {
     uint32_t terrain_id;       // fourth Philox counter word
     int32_t skip_identity;     // skip thermal layers with Kspeed==0 and the
                                // smoothing pass when Kspeed[1]==0 (exact)
+    // rain_mode 3: the reference's rain (glsl/rain.glsl:32-56, hg_terrain_ref.cpp)
+    float rain_time0, rain_time_step;  // frame time of step n: time0 + n * time_step
+    float mountain_thresh, mountain_multip, drops, max_height;
 };
+
+// glsl/rain.glsl's increment of one cell (hg_terrain_ref.cpp)
+float hgo_ref_rain_cell(int x, int y, float total, float time, float amount, float mountain_thresh,
+                        float mountain_multip, float drops, float max_height);
 
 }  // extern "C"
 
@@ -198,6 +205,12 @@ template <typename T> struct World {
 
 #define OMP_ROWS _Pragma("omp parallel for schedule(static)")
 
+// frame time of step n for the reference rain (computed in double, as the
+// library's host does, then rounded to float)
+inline float rain_time(const OracleOptions& o, uint64_t n) {
+    return (float)((double)o.rain_time0 + (double)n * (double)o.rain_time_step);
+}
+
 // glsl/rain.glsl:32-56 (the water increment follows the workload's rain model)
 template <typename T> void rain_pass(World<T>& w, const OracleOptions& o, uint64_t step_1based) {
     const auto& src = w.height.rd();
@@ -209,6 +222,9 @@ template <typename T> void rain_pass(World<T>& w, const OracleOptions& o, uint64
             V4<T> terr = src[w.id(x, y)];
             T incr = T(0);
             if (o.rain_mode == 1) incr = amount;
+            else if (o.rain_mode == 3)
+                incr = T(hgo_ref_rain_cell(x, y, (float)terr.w, rain_time(o, step_1based), o.rain_amount,
+                                           o.mountain_thresh, o.mountain_multip, o.drops, o.max_height));
             else if (rain_word(x, y, step_1based, o.terrain_id, o.rain_seed) < o.rain_threshold) incr = amount;
             terr.z += incr;
             terr.w = terr.x + terr.y + terr.z;

@@ -38,7 +38,10 @@ class OracleErosion(ctypes.Structure):
 class OracleOptions(ctypes.Structure):
     _fields_ = [("rain_mode", ctypes.c_int32), ("rain_period", ctypes.c_int32), ("rain_amount", ctypes.c_float),
                 ("rain_threshold", ctypes.c_uint32), ("rain_seed", ctypes.c_uint64),
-                ("terrain_id", ctypes.c_uint32), ("skip_identity", ctypes.c_int32)]
+                ("terrain_id", ctypes.c_uint32), ("skip_identity", ctypes.c_int32),
+                ("rain_time0", ctypes.c_float), ("rain_time_step", ctypes.c_float),
+                ("mountain_thresh", ctypes.c_float), ("mountain_multip", ctypes.c_float), ("drops", ctypes.c_float),
+                ("max_height", ctypes.c_float)]
 
 
 def build():
@@ -102,8 +105,13 @@ def bernoulli_threshold(p):
     return int(min(max(t, 0), 4294967295))
 
 
-def options(rain_mode=1, period=1, amount=0.01, p=0.0, seed=0, terrain_id=0, skip_identity=1):
-    return OracleOptions(rain_mode, period, amount, bernoulli_threshold(p), seed, terrain_id, skip_identity)
+def options(rain_mode=1, period=1, amount=0.01, p=0.0, seed=0, terrain_id=0, skip_identity=1, time0=0.0,
+            time_step=0.0, mountain_thresh=0.55, mountain_multip=0.05, drops=0.02, max_height=256.0):
+    """Rain and pass options; rain_mode 3 is the reference's rain (frame time
+    time0 + n * time_step at step n, mountain bonus above mountain_thresh of
+    max_height)."""
+    return OracleOptions(rain_mode, period, amount, bernoulli_threshold(p), seed, terrain_id, skip_identity,
+                         time0, time_step, mountain_thresh, mountain_multip, drops, max_height)
 
 
 def settings_config1():
@@ -247,6 +255,46 @@ lib.hgo_adjoint_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, cty
 lib.hgo_forward_ref.restype = ctypes.c_int
 lib.hgo_forward_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+
+
+lib.hgo_ref_heightmap.restype = None
+lib.hgo_ref_heightmap.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+lib.hgo_ref_rain.restype = None
+lib.hgo_ref_rain.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_void_p]
+lib.hgo_ref_simplex.restype = ctypes.c_float
+lib.hgo_ref_simplex.argtypes = [ctypes.c_float, ctypes.c_float]
+lib.hgo_ref_noised.restype = None
+lib.hgo_ref_noised.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_void_p]
+
+
+def ref_heightmap(map_settings, n):
+    """The reference's terrain generator (glsl/heightmap.glsl): (rock, dirt),
+    map_settings any ctypes struct with Map_settings_data's 96-byte layout."""
+    rock = np.empty((n, n), np.float32)
+    dirt = np.empty((n, n), np.float32)
+    lib.hgo_ref_heightmap(ctypes.byref(map_settings), n, rock.ctypes.data, dirt.ctypes.data)
+    return rock, dirt
+
+
+def ref_rain(total, time, rain, max_height):
+    """The reference's rain increment (glsl/rain.glsl) of every cell."""
+    n = total.shape[0]
+    t = np.ascontiguousarray(total, np.float32)
+    out = np.empty((n, n), np.float32)
+    lib.hgo_ref_rain(n, t.ctypes.data, time, rain.amount, rain.mountain_thresh, rain.mountain_multip, rain.drops,
+                     max_height, out.ctypes.data)
+    return out
+
+
+def ref_simplex(x, y):
+    return lib.hgo_ref_simplex(x, y)
+
+
+def ref_noised(x, y):
+    out = (ctypes.c_float * 3)()
+    lib.hgo_ref_noised(x, y, out)
+    return tuple(out)
 
 
 def _adj_settings(s, amount):
