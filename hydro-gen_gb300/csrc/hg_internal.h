@@ -57,6 +57,41 @@ void launch_thermal_out1(const StepConsts& c, const float* rock, const float* di
 void launch_smooth2(const StepConsts& c, const float* rock, const float* dirt, float* rock_o, float* dirt_o,
                     cudaStream_t st);
 
+// ---- particle erosion (hg_particles.cu) --------------------------------------------
+// Droplets as structure of arrays (Particle, glsl/bindings.glsl:101-110).
+struct Drops {
+    int count;
+    float *px, *py, *vx, *vy, *vol;
+    float *s0, *s1;  // sediment of the rock / dirt layer
+    float* sc;       // sediment capacity
+    uint32_t* iters;
+    int32_t* kill;
+};
+// Counting-sort and per-record buffers of one particle world.
+struct ParticleBufs {
+    Drops d;
+    uint32_t* cnt;         // n*n records per texel
+    uint32_t* offs;        // n*n + 1 exclusive prefix
+    uint32_t* cursor;      // n*n scatter cursors
+    uint32_t* block_sums;  // particle_scan_blocks(n*n)
+    uint32_t* keys;        // 4*count records (droplet * 4 + corner), bucketed by texel
+    float* rec;            // 8*count: per record the dirt and rock sediment it left
+    uint8_t* rec_mask;     // 4*count: which layers a record set
+};
+// The fields a particle pass reads or writes; mom = momentum (x, y, z, w).
+struct PWorld {
+    float* rock;
+    float* dirt;
+    float* water;
+    float* mom[4];
+};
+size_t particle_scan_blocks(size_t cells);
+// movement, counting sort, erosion in droplet-id order, sediment replay
+void launch_particle_step(const StepConsts& c, const hg_erosion_settings& es, const ParticleBufs& pb,
+                          const PWorld& pw, uint32_t step1, uint64_t seed, bool should_rain, cudaStream_t st);
+// smoothing with the particle branch: in -> out (all of rock, dirt, water, momentum)
+void launch_particle_smooth(const StepConsts& c, float count, const PWorld& in, const PWorld& out, cudaStream_t st);
+
 // ---- fused step (hg_fused.cu) ---------------------------------------------------
 // Rain settings without the step number (the kernels add the step).
 struct RainBase {

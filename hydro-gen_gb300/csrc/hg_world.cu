@@ -65,6 +65,17 @@ struct Tuning {
     int per_world = 0;  // batches: each world's own launches were faster than one table launch
     double ms_per_world = 0.0;
 };
+
+// Droplets and momentum map of a particle-mode world (hg_particles_init).
+struct Particles {
+    int count = 0;
+    ParticleBufs b{};
+    float* mom[2][4] = {};  // momentum map (x, y, z, w): current, alternate
+    std::vector<void*> allocs;
+    ~Particles() {
+        for (void* p : allocs) cudaFree(p);
+    }
+};
 }  // namespace hg
 
 using namespace hg;
@@ -101,6 +112,7 @@ struct hg_world {
     hg::Tuning tuning;                     // autotuned fused-step variant
     float* red_f = nullptr;   // min/max partials + result
     double* red_d = nullptr;  // FP64 partials + result
+    hg::Particles* parts = nullptr;  // particle mode: droplets and momentum map
 };
 
 struct hg_batch {
@@ -198,6 +210,8 @@ void free_world(hg_world* w) {
     cudaFree(w->s_ero); cudaFree(w->b_ero); cudaFree(w->err); cudaFree(w->d_step);
     for (Plan*& p : w->plans) destroy_plan(p);
     cudaFree(w->red_f); cudaFree(w->red_d);
+    delete w->parts;
+    w->parts = nullptr;
     if (w->stream) cudaStreamDestroy(w->stream);
 }
 
@@ -585,6 +599,8 @@ float* field_ptr(hg_world* w, int field) {
         case HG_FIELD_KS: return w->ks;
         case HG_FIELD_DIRT: return w->dirt[0];
         case HG_FIELD_SEDIMENT_DIRT: return w->sdirt[0];
+        case HG_FIELD_MOMENTUM_X: return w->parts ? w->parts->mom[0][0] : nullptr;
+        case HG_FIELD_MOMENTUM_Y: return w->parts ? w->parts->mom[0][1] : nullptr;
     }
     return nullptr;
 }
@@ -613,6 +629,29 @@ int hg_default_erosion_settings(hg_erosion_settings* out) {
     out->Kspeed[0] = 0.5f; out->Kspeed[1] = 2.0f;
     out->G = 1.0f;
     out->d_t = 0.001f;
+    return HG_OK;
+}
+
+int hg_default_particle_settings(hg_erosion_settings* out) {
+    if (!out) return fail(HG_ERR_INVALID, "null settings");
+    std::memset(out, 0, sizeof(*out));
+    // particle-model defaults, src/state.cpp:61-79 (particle_count left at 0)
+    out->Kc = 0.2f;
+    out->Kalpha[0] = 1.3f; out->Kalpha[1] = 0.6f;
+    out->Kconv = 0.001f;
+    out->Ks[0] = 0.03f; out->Ks[1] = 0.09f;
+    out->Kd[0] = 0.01f; out->Kd[1] = 0.03f;
+    out->Ke = 0.03f;
+    out->Kspeed[0] = 0.002f; out->Kspeed[1] = 0.008f;
+    out->G = 9.81f;
+    out->d_t = 0.25f;
+    out->density = 1.0f;
+    out->init_volume = 1.0f;
+    out->friction = 0.2f;
+    out->inertia = 1.0f;
+    out->min_volume = 0.0f;
+    out->min_velocity = 0.001f;
+    out->ttl = 15000;
     return HG_OK;
 }
 
@@ -732,7 +771,8 @@ int hg_world_stream(const hg_world* w, void** stream) {
 int hg_set_erosion_settings(hg_world* w, const hg_erosion_settings* s) {
     HG_CHECK_WORLD(w);
     if (!s) return fail(HG_ERR_INVALID, "null settings");
-    if (s->particle_count != 0) return fail(HG_ERR_INVALID, "particle_count must be 0 for the grid model");
+    if (s->particle_count != 0 && (!w->parts || s->particle_count != (uint32_t)w->parts->count))
+        return fail(HG_ERR_INVALID, "particle_count must be 0 or the droplet count of hg_particles_init");
     if (!(s->d_t > 0.0f) || !std::isfinite(s->d_t)) return fail(HG_ERR_INVALID, "d_t must be positive and finite");
     if (w->layers == 1 && s->Kconv != 0.0f)
         return fail(HG_ERR_INVALID, "Kconv must be 0 in a one-layer world (no dirt layer)");
@@ -773,6 +813,20 @@ int hg_set_step_options(hg_world* w, const hg_step_options* o) {
 }
 
 namespace {
+// idle droplets, zero momentum map
+int reset_particles(hg_world* w) {
+    Particles& P = *w->parts;
+    const size_t cnt = (size_t)P.count, bytes = cells(w) * sizeof(float);
+    const Drops& d = P.b.d;
+    for (float* f : {d.px, d.py, d.vx, d.vy, d.vol, d.s0, d.s1, d.sc})
+        HG_CUDA(cudaMemsetAsync(f, 0, cnt * sizeof(float), w->stream));
+    HG_CUDA(cudaMemsetAsync(d.iters, 0, cnt * sizeof(uint32_t), w->stream));
+    HG_CUDA(cudaMemsetAsync(d.kill, 0, cnt * sizeof(int32_t), w->stream));
+    for (int k = 0; k < 2; ++k)
+        for (int c = 0; c < 4; ++c) HG_CUDA(cudaMemsetAsync(P.mom[k][c], 0, bytes, w->stream));
+    return HG_OK;
+}
+
 // every state field (and the dirt layer's) back to zero
 int zero_state(hg_world* w) {
     size_t bytes = cells(w) * sizeof(float);
@@ -787,6 +841,7 @@ int zero_state(hg_world* w) {
         HG_CUDA(cudaMemsetAsync(w->dirt[k], 0, bytes, w->stream));
         HG_CUDA(cudaMemsetAsync(w->sdirt[k], 0, bytes, w->stream));
     }
+    if (w->parts) return reset_particles(w);
     return HG_OK;
 }
 
@@ -843,6 +898,81 @@ int hg_init_reference_heightmap(hg_world* w, const hg_map_settings* s) {
     w->version += 1;
     w->step = 0;
     w->dev_step_valid = false;
+    return HG_OK;
+}
+
+int hg_particles_init(hg_world* w, int count) {
+    HG_CHECK_WORLD(w);
+    if (w->layers != 2) return fail(HG_ERR_UNSUPPORTED, "particle erosion runs on two-layer worlds");
+    if (count < 1 || count > (1 << 28)) return fail(HG_ERR_INVALID, "count must be in [1, 2^28]");
+    DeviceGuard g(w->device);
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    delete w->parts;
+    w->parts = nullptr;
+    Particles* P = new (std::nothrow) Particles();
+    if (!P) return fail(HG_ERR_OOM, "host allocation failed");
+    const size_t cnt = (size_t)count, cl = cells(w);
+    cudaError_t e = cudaSuccess;
+    auto take = [&](size_t bytes) -> void* {
+        void* p = nullptr;
+        if (e == cudaSuccess) e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) P->allocs.push_back(p);
+        return e == cudaSuccess ? p : nullptr;
+    };
+    Drops& d = P->b.d;
+    d.count = count;
+    float** fs[8] = {&d.px, &d.py, &d.vx, &d.vy, &d.vol, &d.s0, &d.s1, &d.sc};
+    for (float** f : fs) *f = (float*)take(cnt * sizeof(float));
+    d.iters = (uint32_t*)take(cnt * sizeof(uint32_t));
+    d.kill = (int32_t*)take(cnt * sizeof(int32_t));
+    P->b.cnt = (uint32_t*)take(cl * sizeof(uint32_t));
+    P->b.offs = (uint32_t*)take((cl + 1) * sizeof(uint32_t));
+    P->b.cursor = (uint32_t*)take(cl * sizeof(uint32_t));
+    P->b.block_sums = (uint32_t*)take(particle_scan_blocks(cl) * sizeof(uint32_t));
+    P->b.keys = (uint32_t*)take(4 * cnt * sizeof(uint32_t));
+    P->b.rec = (float*)take(8 * cnt * sizeof(float));
+    P->b.rec_mask = (uint8_t*)take(4 * cnt);
+    for (int k = 0; k < 2; ++k)
+        for (int c = 0; c < 4; ++c) P->mom[k][c] = (float*)take(cl * sizeof(float));
+    if (e != cudaSuccess) {
+        delete P;
+        cudaGetLastError();
+        return fail(e == cudaErrorMemoryAllocation ? HG_ERR_OOM : HG_ERR_CUDA,
+                    std::string("particle allocation: ") + cudaGetErrorString(e));
+    }
+    P->count = count;
+    w->parts = P;
+    int rc = reset_particles(w);
+    if (rc != HG_OK) return rc;
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    return HG_OK;
+}
+
+int hg_particles_get(hg_world* w, float* state8, uint32_t* iters, int32_t* kill) {
+    HG_CHECK_WORLD(w);
+    if (!w->parts) return fail(HG_ERR_INVALID, "no droplets: call hg_particles_init first");
+    DeviceGuard g(w->device);
+    const Drops& d = w->parts->b.d;
+    const size_t cnt = (size_t)d.count;
+    if (state8) {
+        std::vector<float> col(cnt);
+        const float* fs[8] = {d.px, d.py, d.vx, d.vy, d.vol, d.s0, d.s1, d.sc};
+        for (int k = 0; k < 8; ++k) {
+            HG_CUDA(cudaMemcpyAsync(col.data(), fs[k], cnt * sizeof(float), cudaMemcpyDeviceToHost, w->stream));
+            HG_CUDA(cudaStreamSynchronize(w->stream));
+            for (size_t i = 0; i < cnt; ++i) state8[8 * i + k] = col[i];
+        }
+    }
+    if (iters) HG_CUDA(cudaMemcpyAsync(iters, d.iters, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    if (kill) HG_CUDA(cudaMemcpyAsync(kill, d.kill, cnt * sizeof(int32_t), cudaMemcpyDeviceToHost, w->stream));
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    return HG_OK;
+}
+
+int hg_particles_count(const hg_world* w, int* count) {
+    HG_CHECK_WORLD(w);
+    if (!count) return fail(HG_ERR_INVALID, "null output");
+    *count = w->parts ? w->parts->count : 0;
     return HG_OK;
 }
 
@@ -952,11 +1082,46 @@ int hg_world_set_step(hg_world* w, uint64_t step) {
 int hg_step(hg_world* w, int nsteps, int mode) {
     HG_CHECK_WORLD(w);
     if (nsteps < 0) return fail(HG_ERR_INVALID, "nsteps must be >= 0");
-    if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED) return fail(HG_ERR_INVALID, "bad mode");
+    if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_PARTICLES)
+        return fail(HG_ERR_INVALID, "bad mode");
     DeviceGuard g(w->device);
     StepConsts c = make_consts(w);
     cudaStream_t st = w->stream;
     auto swap = [&](int f) { float* t = w->cur[f]; w->cur[f] = w->alt[f]; w->alt[f] = t; };
+    if (mode == HG_MODE_PARTICLES) {
+        // Erosion::dispatch_particle (src/erosion.cpp:132-156): droplets move
+        // and erode, both thermal layers (identities skipped), smoothing with
+        // the momentum fold; rain on = new droplets spawn
+        if (!w->parts) return fail(HG_ERR_INVALID, "particle mode needs hg_particles_init");
+        Particles& P = *w->parts;
+        auto swap2 = [](float** f) { float* t = f[0]; f[0] = f[1]; f[1] = t; };
+        for (int k = 0; k < nsteps; ++k) {
+            PWorld cur{w->cur[S_ROCK], w->dirt[0], w->cur[S_WATER], {P.mom[0][0], P.mom[0][1], P.mom[0][2], P.mom[0][3]}};
+            launch_particle_step(c, w->es, P.b, cur, (uint32_t)(w->step + 1), w->opt.rain_seed,
+                                 w->opt.rain_mode != HG_RAIN_OFF, st);
+            if (c.thermal) {
+                launch_thermal_out(c, w->cur[S_ROCK], w->tc, w->td, st);
+                launch_thermal_in(c, w->cur[S_ROCK], w->tc, w->td, w->alt[S_ROCK], st);
+                swap(S_ROCK);
+            }
+            if (c.Kspeed1 != 0.0f) {
+                launch_thermal_out1(c, w->cur[S_ROCK], w->dirt[0], w->tc, w->td, st);
+                launch_thermal_in(c, w->dirt[0], w->tc, w->td, w->dirt[1], st);
+                swap2(w->dirt);
+            }
+            PWorld in{w->cur[S_ROCK], w->dirt[0], w->cur[S_WATER], {P.mom[0][0], P.mom[0][1], P.mom[0][2], P.mom[0][3]}};
+            PWorld out{w->alt[S_ROCK], w->dirt[1], w->alt[S_WATER], {P.mom[1][0], P.mom[1][1], P.mom[1][2], P.mom[1][3]}};
+            launch_particle_smooth(c, (float)P.count, in, out, st);
+            swap(S_ROCK);
+            swap(S_WATER);
+            swap2(w->dirt);
+            for (int ch = 0; ch < 4; ++ch) std::swap(P.mom[0][ch], P.mom[1][ch]);
+            w->step += 1;
+        }
+        if (nsteps > 0) w->dev_step_valid = false;
+        HG_CUDA(cudaGetLastError());
+        return HG_OK;
+    }
     if (mode == HG_MODE_PLAIN && w->layers == 2) {
         // the reference's two-layer step (src/erosion.cpp:158-200): thermal
         // and smoothing passes for layers whose slippage rate is 0 are

@@ -26,9 +26,10 @@ STATUS = {-1: "HG_ERR_INVALID", -2: "HG_ERR_OOM", -3: "HG_ERR_CUDA", -4: "HG_ERR
           -5: "HG_ERR_UNSUPPORTED", -6: "HG_ERR_IO", -7: "HG_ERR_STATE"}
 HG_AUTO = -1
 RAIN_OFF, RAIN_UNIFORM, RAIN_BERNOULLI, RAIN_REFERENCE = 0, 1, 2, 3
-MODE_PLAIN, MODE_FUSED, MODE_FUSED_PER_WORLD = 0, 1, 2
+MODE_PLAIN, MODE_FUSED, MODE_FUSED_PER_WORLD, MODE_PARTICLES = 0, 1, 2, 3
 FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_t": 5, "flux_b": 6,
-          "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10, "dirt": 11, "sediment_dirt": 12}
+          "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10, "dirt": 11, "sediment_dirt": 12,
+          "momentum_x": 13, "momentum_y": 14}
 STATE_FIELDS = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"]
 
 
@@ -123,6 +124,10 @@ def _load():
         "hg_default_map_settings": (ctypes.c_int, [ctypes.POINTER(MapSettings)]),
         "hg_set_map_settings": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
         "hg_init_reference_heightmap": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
+        "hg_particles_init": (ctypes.c_int, [P, ctypes.c_int]),
+        "hg_default_particle_settings": (ctypes.c_int, [ctypes.POINTER(ErosionSettings)]),
+        "hg_particles_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
+        "hg_particles_get": (ctypes.c_int, [P, P, P, P]),
         "hg_selftest_division": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
         "hg_batch_launch_form": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
         "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
@@ -185,6 +190,13 @@ def settings_config2():
     """Config-1 physics with thermal erosion: talus tan 0.65, slippage 0.3."""
     s = settings_config1()
     s.Kspeed[0] = 0.3
+    return s
+
+
+def settings_particles():
+    """The reference's particle-model defaults (src/state.cpp:61-79)."""
+    s = ErosionSettings()
+    check(lib.hg_default_particle_settings(ctypes.byref(s)))
     return s
 
 
@@ -279,6 +291,20 @@ class World:
 
     def set_map(self, ms):
         check(lib.hg_set_map_settings(self.h, ctypes.byref(ms)))
+
+    def particles_init(self, count):
+        """`count` idle droplets and a zero momentum map (two-layer worlds)."""
+        check(lib.hg_particles_init(self.h, count))
+
+    def particles(self):
+        """(state[count, 8] = x, y, vx, vy, volume, rock sed, dirt sed, capacity; iters; kill)"""
+        c = ctypes.c_int()
+        check(lib.hg_particles_count(self.h, ctypes.byref(c)))
+        st = np.empty((c.value, 8), np.float32)
+        it = np.empty(c.value, np.uint32)
+        kl = np.empty(c.value, np.int32)
+        check(lib.hg_particles_get(self.h, st.ctypes.data, it.ctypes.data, kl.ctypes.data))
+        return st, it, kl
 
     def init_ks_field(self, ns, base, k):
         check(lib.hg_init_ks_field(self.h, ctypes.byref(ns), base, k))

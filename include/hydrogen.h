@@ -43,7 +43,7 @@ extern "C" {
  * bytes unchanged.  Index [0] is the rock layer, [1] the dirt layer
  * (src/rendering.cpp:214).  Kalpha is the talus angle in radians. */
 typedef struct hg_erosion_settings {
-    uint32_t particle_count; /*  0  must be 0: grid model */
+    uint32_t particle_count; /*  0  0, or the droplet count of hg_particles_init */
     float Kc;                /*  4  sediment capacity */
     float Kalpha[2];         /*  8  talus angle per layer (radians) */
     float Kconv;             /* 16  rock->dirt sediment conversion */
@@ -160,11 +160,14 @@ typedef struct hg_noise_settings {
 #define HG_FIELD_KS 10       /* per-cell rock solubility (replaces Ks[0]) */
 #define HG_FIELD_DIRT 11     /* heightmap.g: dirt layer (two-layer worlds) */
 #define HG_FIELD_SEDIMENT_DIRT 12 /* sedimap.g: suspended dirt (two-layer worlds) */
-#define HG_FIELD_COUNT 13
+#define HG_FIELD_MOMENTUM_X 13    /* momentmap.x: droplet momentum map (particle mode) */
+#define HG_FIELD_MOMENTUM_Y 14    /* momentmap.y */
+#define HG_FIELD_COUNT 15
 
 #define HG_MODE_PLAIN 0           /* one kernel per GLSL pass */
 #define HG_MODE_FUSED 1           /* two fused, tiled kernels per step */
 #define HG_MODE_FUSED_PER_WORLD 2 /* batches only: each world's own fused launches */
+#define HG_MODE_PARTICLES 3       /* droplet erosion (hg_particles_init; two-layer worlds) */
 
 typedef struct hg_world hg_world;
 
@@ -177,6 +180,9 @@ uint64_t hg_launch_count(void);
 
 /* Reference grid-model defaults (src/state.cpp:81-92). */
 int hg_default_erosion_settings(hg_erosion_settings* out);
+/* Reference particle-model defaults (src/state.cpp:61-79), particle_count 0
+ * (hg_set_erosion_settings takes 0 or the world's droplet count). */
+int hg_default_particle_settings(hg_erosion_settings* out);
 /* Reference rain defaults (src/settings.hpp:16-21). */
 int hg_default_rain_settings(hg_rain_settings* out);
 int hg_default_step_options(hg_step_options* out);
@@ -207,6 +213,28 @@ int hg_set_map_settings(hg_world* w, const hg_map_settings* s);
  * settings, zeroes water, sediment, flux and velocity, resets the step
  * counter. */
 int hg_init_reference_heightmap(hg_world* w, const hg_map_settings* s);
+/* The reference's "particle" erosion type (ParticleBuffer, src/state.cpp:28-30;
+ * Erosion::dispatch_particle, src/erosion.cpp:132-156): allocates `count`
+ * idle droplets (1 <= count <= 2^28) and the momentum map of a two-layer
+ * world, or resets them.  hg_step(w, n, HG_MODE_PARTICLES) then runs per
+ * step: droplet movement (glsl/particle.glsl:64-136; new droplets spawn
+ * while rain_mode != HG_RAIN_OFF, the reference's should_rain), droplet
+ * erosion (glsl/particle_erosion.glsl:22-128), the thermal passes of both
+ * layers and smoothing with the momentum fold (glsl/smoothing.glsl:22-103).
+ * The droplets' updates of a texel apply in droplet-id order (the reference
+ * takes a per-texel spinlock in whatever order droplets arrive), and spawn
+ * positions come from Philox4x32-10 (counter: droplet id, step, 0x70617274,
+ * 0; key: rain_seed) instead of the reference's fract(1e4 sin(...)) hash.
+ * The reference dispatches count / work-group-size whole groups; every
+ * droplet runs here. */
+int hg_particles_init(hg_world* w, int count);
+/* Number of droplets (0 before hg_particles_init). */
+int hg_particles_count(const hg_world* w, int* count);
+/* Droplet state to host memory (any pointer may be NULL): state8 gets 8
+ * floats per droplet (x, y, vx, vy, volume, rock sediment, dirt sediment,
+ * capacity), iters the age in steps (0: idle), kill 1 for a droplet that
+ * respawns on the next step. */
+int hg_particles_get(hg_world* w, float* state8, uint32_t* iters, int32_t* kill);
 /* Replaces State::World::delete_textures (src/state.cpp:46-55). */
 int hg_world_destroy(hg_world* w);
 int hg_world_size(const hg_world* w, int* n);
@@ -215,8 +243,9 @@ int hg_world_stream(const hg_world* w, void** stream);
 
 /* Replaces Erosion_settings::push_data / "Set Erosion settings"
  * (src/settings.hpp:64-66, src/rendering.cpp:303-305).  Takes effect at the
- * next step.  Rejects particle_count != 0, d_t <= 0 and, for one-layer
- * worlds, Kconv != 0 or Kspeed[1] != 0 (those need the dirt layer). */
+ * next step.  Rejects a particle_count other than 0 or the world's droplet
+ * count, d_t <= 0 and, for one-layer worlds, Kconv != 0 (it needs the dirt
+ * layer). */
 int hg_set_erosion_settings(hg_world* w, const hg_erosion_settings* s);
 int hg_get_erosion_settings(const hg_world* w, hg_erosion_settings* s);
 /* Replaces Rain_settings::push_data (src/settings.hpp:22-24). */

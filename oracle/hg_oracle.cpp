@@ -195,6 +195,15 @@ template <typename T> struct World {
     Pair<T> thc;         // thermal cross outflow (L, R, T, B)
     Pair<T> thd;         // thermal diagonal outflow (LT, RT, LB, RB)
     std::vector<float> ks;  // optional per-cell rock solubility (replaces Ks[0])
+    // particle mode (glsl/particle.glsl): Particle (glsl/bindings.glsl:101-110)
+    struct Drop {
+        float sc = 0;
+        uint32_t iters = 0;
+        float px = 0, py = 0, vx = 0, vy = 0, vol = 0;
+        float sed[2] = {0, 0};
+        bool kill = false;
+    };
+    std::vector<Drop> drops;
     World(int n_) : n(n_) {
         size_t c = (size_t)n * n;
         height.init(c); flux.init(c); vel.init(c); sed.init(c); thc.init(c); thd.init(c);
@@ -563,6 +572,222 @@ template <typename T> void one_step(World<T>& w, const OracleErosion& s, const O
     w.step = n1;
 }
 
+// ---- particle mode: src/erosion.cpp:132-156 ------------------------------------
+// The reference spawns droplets at fract(1e4 sin(...))-hashed positions keyed
+// by the frame time; no two libms agree on those sines, so spawn positions
+// here come from Philox4x32-10 with counter (particle id, step, 'part', 0)
+// and the rain seed as key, a 24-bit uniform per axis.
+inline float spawn_uniform(uint32_t word) { return (float)(word >> 8) * 0x1p-24f; }
+
+// img_bilinear (glsl/img_interpolation.glsl:3-22) of one channel, 0 outside
+inline float bilin(const World<float>& w, const std::vector<V4<float>>& img, int ch, float sx, float sy) {
+    int ix = (int)sx, iy = (int)sy;
+    float fx = gfract(sx), fy = gfract(sy);
+    auto f = [&](int xx, int yy) -> float { return w.inb(xx, yy) ? img[w.id(xx, yy)][ch] : 0.0f; };
+    float v1 = gmix(f(ix, iy), f(ix + 1, iy), fx);
+    float v2 = gmix(f(ix, iy + 1), f(ix + 1, iy + 1), fx);
+    return gmix(v1, v2, fy);
+}
+
+// glsl/particle.glsl:64-136
+void particle_move_pass(World<float>& w, const OracleErosion& s, bool should_rain, uint64_t step1, uint64_t seed) {
+    const auto& H = w.height.rd();
+    const auto& M = w.vel.rd();
+    const float dt = s.d_t;
+    const float span = (float)w.n - 4.0f;
+    for (size_t id = 0; id < w.drops.size(); ++id) {
+        auto p = w.drops[id];
+        if (p.iters == 0 && !should_rain) continue;
+        for (int i = 0; i < 2; ++i)
+            if (p.sed[i] < 0.0f || p.iters == 0) p.sed[i] = 0.0f;
+        if (p.iters == 0 || p.kill) {
+            uint32_t ctr[4] = {(uint32_t)id, (uint32_t)step1, 0x70617274u, 0u};
+            uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+            uint32_t out[4];
+            philox4x32_10(ctr, key, out);
+            p.kill = false;
+            p.px = spawn_uniform(out[0]) * span / 1.0f + 2.0f;
+            p.py = spawn_uniform(out[1]) * span / 1.0f + 2.0f;
+            p.vx = 0.0f;
+            p.vy = 0.0f;
+            p.vol = s.init_volume;
+            p.iters = should_rain ? 1u : 0u;
+            if (!should_rain) { w.drops[id] = p; continue; }
+        }
+        // get_terr_normal (:48-60)
+        float rr = bilin(w, H, 0, p.px + 1.0f, p.py), rg = bilin(w, H, 1, p.px + 1.0f, p.py);
+        float lr = bilin(w, H, 0, p.px - 1.0f, p.py), lg = bilin(w, H, 1, p.px - 1.0f, p.py);
+        float br = bilin(w, H, 0, p.px, p.py - 1.0f), bg = bilin(w, H, 1, p.px, p.py - 1.0f);
+        float tr = bilin(w, H, 0, p.px, p.py + 1.0f), tg = bilin(w, H, 1, p.px, p.py + 1.0f);
+        float dx = rr + rg - lr - lg;
+        float dz = tr + tg - br - bg;
+        float cx = dx * 2.0f - 0.0f * dz, cy = 0.0f * 0.0f - 2.0f * 2.0f, cz = 2.0f * dz - dx * 0.0f;
+        float len = std::sqrt(cx * cx + cy * cy + cz * cz);
+        float nx = cx / len, ny = cy / len, nz = cz / len;
+        float mx = bilin(w, M, 0, p.px, p.py), my = bilin(w, M, 1, p.px, p.py);
+        float water = bilin(w, H, 2, p.px, p.py);
+        p.vx -= (dt * nx) / p.vol * s.G;
+        p.vy -= (dt * nz) / p.vol * s.G;
+        float lm = std::sqrt(mx * mx + my * my), lv = std::sqrt(p.vx * p.vx + p.vy * p.vy);
+        if (lm > 0.0f && lv > 0.0f) {
+            float d = (mx / lm) * (p.vx / lv) + (my / lm) * (p.vy / lv);
+            float k = s.inertia * d / (p.vol + 1e5f * water);
+            p.vx += k * mx;
+            p.vy += k * my;
+        }
+        lv = std::sqrt(p.vx * p.vx + p.vy * p.vy);
+        if (lv > 1.0f) { p.vx = p.vx / lv; p.vy = p.vy / lv; }
+        float ox = p.px, oy = p.py;
+        p.px += dt * p.vx;
+        p.py += dt * p.vy;
+        if (p.px <= 1.0f || p.py <= 1.0f || p.px * 1.0f >= (float)(w.n - 2) || p.py * 1.0f >= (float)(w.n - 2)) {
+            p.px = ox; p.py = oy; p.vx = 0.0f; p.vy = 0.0f; p.kill = true;
+        }
+        float fr = 1.0f - dt * s.friction * ny;
+        p.vx *= fr;
+        p.vy *= fr;
+        p.vol -= dt * s.Ke;
+        float sin_a = std::fabs(std::sqrt(1.0f - ny * ny));
+        lv = std::sqrt(p.vx * p.vx + p.vy * p.vy);
+        p.sc = gmax(0.0f, s.Kc * p.vol * lv * gmax(0.02f, sin_a));
+        p.iters++;
+        if (p.vol <= s.min_volume || lv < s.min_velocity || p.iters >= s.ttl) p.kill = true;
+        w.drops[id] = p;
+    }
+}
+
+// glsl/particle_erosion.glsl:22-128, particles in id order, corners 0..3
+void particle_erosion_pass(World<float>& w, const OracleErosion& s) {
+    auto& H = w.height.tex[w.height.r];
+    auto& M = w.vel.tex[w.vel.r];
+    for (size_t id = 0; id < w.drops.size(); ++id) {
+        if (w.drops[id].iters == 0) continue;
+        const float px = w.drops[id].px, py = w.drops[id].py;
+        const int bx = (int)(px * 1.0f), by = (int)(py * 1.0f);
+        const float ofx = gfract(px * 1.0f), ofy = gfract(py * 1.0f);
+        const int cxs[4] = {bx, bx + 1, bx + 1, bx}, cys[4] = {by, by, by + 1, by + 1};
+        const float wx[4] = {1.0f - ofx, ofx, ofx, 1.0f - ofx}, wy[4] = {1.0f - ofy, 1.0f - ofy, ofy, ofy};
+        const float old_sed[2] = {w.drops[id].sed[0], w.drops[id].sed[1]};
+        for (int k = 0; k < 4; ++k) {
+            auto part = w.drops[id];
+            V4<float> terr = H[w.id(cxs[k], cys[k])];
+            V4<float> mom = M[w.id(cxs[k], cys[k])];
+            const float multipl = wx[k] * wy[k];
+            float cap = 0.0f;
+            for (int i = 1; i >= 0; --i) {
+                if (part.kill) {
+                    float sed = old_sed[i] * multipl;
+                    terr[i] += sed;
+                    part.sed[i] -= sed;
+                    continue;
+                }
+                const float Kls = s.d_t * s.Ks[i], Kld = s.d_t * s.Kd[i];
+                const float c = gmax(0.0f, part.sc - cap);
+                float s1 = old_sed[i];
+                const float old_terr = terr[i];
+                if (c > s1) {
+                    float eroded = multipl * Kls * (c - s1);
+                    s1 += eroded;
+                    terr[i] -= eroded;
+                    if (terr[i] < 0.0f) {
+                        s1 += terr[i];
+                        terr[i] = 0.0f;
+                        cap += old_terr;
+                    } else {
+                        part.sed[i] = s1;
+                        break;
+                    }
+                } else {
+                    float deposit = multipl * Kld * (s1 - c);
+                    s1 -= deposit;
+                    terr[i] += deposit;
+                }
+                part.sed[i] = s1;
+            }
+            float conv = part.sed[0] * s.Kconv * s.d_t;
+            part.sed[1] += conv;
+            part.sed[0] -= conv;
+            w.drops[id] = part;
+            terr.z += 1e-5f * part.vol * multipl;
+            terr.w = terr.x + terr.z + terr.y;
+            mom.z += part.vol * part.vx * multipl;
+            mom.w += part.vol * part.vy * multipl;
+            H[w.id(cxs[k], cys[k])] = terr;
+            M[w.id(cxs[k], cys[k])] = mom;
+        }
+    }
+}
+
+// glsl/smoothing.glsl:22-103 with the particle branch (:76-95): both layers,
+// the drops' momentum folded into the momentum map, water display decay.
+// Border texels copy their height and leave the momentum map's write buffer
+// as it was.
+void particle_smoothing_pass(World<float>& w, const OracleErosion& s) {
+    const auto& H = w.height.rd();
+    auto& Ho = w.height.wr();
+    const auto& M = w.vel.rd();
+    auto& Mo = w.vel.wr();
+    const int n = w.n;
+    const float count = (float)w.drops.size();
+    for (int y = 0; y < n; ++y)
+        for (int x = 0; x < n; ++x) {
+            V4<float> terrain = H[w.id(x, y)];
+            float tr = terrain.x, tg = terrain.y;
+            if (x == 0 || y == 0 || x == n - 1 || y == n - 1) {
+                Ho[w.id(x, y)] = terrain;
+                continue;
+            }
+            V4<float> L4 = H[w.id(x - 1, y)], R4 = H[w.id(x + 1, y)], T4 = H[w.id(x, y + 1)], B4 = H[w.id(x, y - 1)];
+            float lr = L4.x, lg = L4.y, rr = R4.x, rg = R4.y, trr = T4.x, tgg = T4.y, br = B4.x, bg = B4.y;
+            float dlr = tr - lr, dlg = tg - lg; dlg += dlr;
+            float drr = tr - rr, drg = tg - rg; drg += drr;
+            float dtr = tr - trr, dtg = tg - tgg; dtg += dtr;
+            float dbr = tr - br, dbg = tg - bg; dbg += dbr;
+            float g_hdiff = std::fabs((dlg + drg + dtg + dbg) / 4.0f);
+            float r_hdiff = std::fabs((dlr + drr + dtr + dbr) / 4.0f);
+            float xr = dlr * drr, xg = dlg * drg, yr = dtr * dbr, yg = dtg * dbg;
+            float nr = tr, ng = tg;
+            if ((((-dlr) > r_hdiff || (-drr) > r_hdiff) && xr > 0) || (((-dtr) > r_hdiff || (-dbr) > r_hdiff) && yr > 0))
+                nr = (tr + lr + rr + trr + br) / 5.0f;
+            if ((((-dlg) > g_hdiff || (-drg) > g_hdiff) && xg > 0) || (((-dtg) > g_hdiff || (-dbg) > g_hdiff) && yg > 0))
+                ng = (tg + lg + rg + tgg + bg) / 5.0f;
+            float multip = gclamp(s.Kspeed[1] * s.d_t, 0.0f, 1.0f);
+            V4<float> mom = M[w.id(x, y)];
+            const float keep = gclamp(1.0f - 1e-12f * count, 0.0f, 1.0f);
+            mom.x *= keep;
+            mom.y *= keep;
+            mom.x += 1e-12f * count * mom.z;
+            mom.y += 1e-12f * count * mom.w;
+            mom.z = 0.0f;
+            mom.w = 0.0f;
+            terrain.z *= gclamp(1.0f - 8e-8f * count, 0.0f, 1.0f);
+            if (terrain.z < 1e-6f) terrain.z = 0.0f;
+            if (std::sqrt(mom.x * mom.x + mom.y * mom.y) < 1e-12f) { mom.x = 0.0f; mom.y = 0.0f; }
+            Mo[w.id(x, y)] = mom;
+            terrain.x = multip * nr + (1.0f - multip) * terrain.x;
+            terrain.y = multip * ng + (1.0f - multip) * terrain.y;
+            terrain.w = terrain.x + terrain.y + terrain.z;
+            Ho[w.id(x, y)] = terrain;
+        }
+    w.height.swap();
+    w.vel.swap();
+}
+
+// Erosion::dispatch_particle (src/erosion.cpp:132-156): movement, erosion,
+// thermal layers, smoothing
+void particle_step(World<float>& w, const OracleErosion& s, const OracleOptions& o) {
+    uint64_t n1 = w.step + 1;
+    particle_move_pass(w, s, o.rain_mode != 0, n1, o.rain_seed);
+    particle_erosion_pass(w, s);
+    for (int layer = 0; layer < 2; ++layer) {
+        if (o.skip_identity && s.Kspeed[layer] == 0.0f) continue;
+        thermal_flux_pass(w, s, layer);
+        thermal_transport_pass(w, layer);
+    }
+    particle_smoothing_pass(w, s);
+    w.step = n1;
+}
+
 // ---- simplex fBm (own 2-D simplex, Gustavson 2005 "Simplex noise demystified")
 inline uint32_t fmix32(uint32_t h) {  // MurmurHash3 finaliser (Appleby, public domain)
     h ^= h >> 16; h *= 0x85ebca6bu; h ^= h >> 13; h *= 0xc2b2ae35u; h ^= h >> 16;
@@ -610,7 +835,7 @@ inline float simplex2f(float x, float y, uint32_t seed) {
 // ---- C interface (ctypes) ---------------------------------------------------
 extern "C" {
 
-enum { F_ROCK = 0, F_WATER, F_SED, F_FL, F_FR, F_FT, F_FB, F_U, F_V, F_DIRT, F_SED_DIRT, F_VZ, F_TOTAL, F_COUNT };
+enum { F_ROCK = 0, F_WATER, F_SED, F_FL, F_FR, F_FT, F_FB, F_U, F_V, F_DIRT, F_SED_DIRT, F_VZ, F_TOTAL, F_VW, F_COUNT };
 
 struct OracleHandle {
     int prec;
@@ -651,6 +876,7 @@ template <typename T> static T* chan(World<T>& w, int field, size_t i, bool writ
         case F_U: return &w.vel.tex[w.vel.r][i].x;
         case F_V: return &w.vel.tex[w.vel.r][i].y;
         case F_VZ: return &w.vel.tex[w.vel.r][i].z;
+        case F_VW: return &w.vel.tex[w.vel.r][i].w;
     }
     return nullptr;
 }
@@ -714,6 +940,36 @@ int hgo_step(void* p, const OracleErosion* s, const OracleOptions* o, int nsteps
     for (int k = 0; k < nsteps; ++k) {
         if (h->wd) one_step(*h->wd, *s, *o);
         else one_step(*h->wf, *s, *o);
+    }
+    return 0;
+}
+
+// particle mode (precision 32): `count` droplets, all idle
+int hgo_particles_init(void* p, int count) {
+    auto* h = (OracleHandle*)p;
+    if (!h || !h->wf || count < 0) return -1;
+    h->wf->drops.assign((size_t)count, World<float>::Drop{});
+    return 0;
+}
+
+int hgo_particle_step(void* p, const OracleErosion* s, const OracleOptions* o, int nsteps) {
+    auto* h = (OracleHandle*)p;
+    if (!h || !h->wf || !s || !o || nsteps < 0) return -1;
+    for (int k = 0; k < nsteps; ++k) particle_step(*h->wf, *s, *o);
+    return 0;
+}
+
+// droplet state: 8 floats each (x, y, vx, vy, volume, rock sediment, dirt
+// sediment, capacity) and iters / kill flag
+int hgo_particles_get(void* p, float* state8, uint32_t* iters, int32_t* kill) {
+    auto* h = (OracleHandle*)p;
+    if (!h || !h->wf) return -1;
+    for (size_t i = 0; i < h->wf->drops.size(); ++i) {
+        const auto& d = h->wf->drops[i];
+        float* o = state8 + 8 * i;
+        o[0] = d.px; o[1] = d.py; o[2] = d.vx; o[3] = d.vy; o[4] = d.vol; o[5] = d.sed[0]; o[6] = d.sed[1]; o[7] = d.sc;
+        iters[i] = d.iters;
+        kill[i] = d.kill ? 1 : 0;
     }
     return 0;
 }

@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libhg_oracle.so")
 
 FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_t": 5, "flux_b": 6,
-          "vel_u": 7, "vel_v": 8, "dirt": 9, "sediment_dirt": 10, "vel_z": 11, "total": 12}
+          "vel_u": 7, "vel_v": 8, "dirt": 9, "sediment_dirt": 10, "vel_z": 11, "total": 12, "vel_w": 13}
 PASSES = {"rain": 0, "flux": 1, "erosion": 2, "sediment": 3, "thermal_flux": 4, "thermal_transport": 5,
           "smoothing": 6}
 
@@ -80,6 +80,10 @@ def _load():
                                ctypes.c_float, ctypes.c_float]),
         "hgo_fbm_scaled": (None, [P, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+        "hgo_particles_init": (ctypes.c_int, [P, ctypes.c_int]),
+        "hgo_particle_step": (ctypes.c_int, [P, ctypes.POINTER(OracleErosion), ctypes.POINTER(OracleOptions),
+                                             ctypes.c_int]),
+        "hgo_particles_get": (ctypes.c_int, [P, P, P, P]),
         "hgo_num_threads": (ctypes.c_int, []),
         "hgo_set_num_threads": (None, [ctypes.c_int]),
     }
@@ -200,6 +204,22 @@ class OracleWorld:
     def run_pass(self, name, settings, opts=None, layer=0):
         opts = opts or options()
         assert lib.hgo_pass(self.h, ctypes.byref(settings), ctypes.byref(opts), PASSES[name], layer) == 0
+
+    def particles_init(self, count):
+        assert lib.hgo_particles_init(self.h, count) == 0
+        self.count_particles = count
+
+    def particle_step(self, settings, opts, nsteps=1):
+        assert lib.hgo_particle_step(self.h, ctypes.byref(settings), ctypes.byref(opts), nsteps) == 0
+
+    def particles(self):
+        """(state[count, 8] = x, y, vx, vy, volume, rock sed, dirt sed, capacity; iters; kill)"""
+        c = self.count_particles
+        st = np.empty((c, 8), np.float32)
+        it = np.empty(c, np.uint32)
+        kl = np.empty(c, np.int32)
+        assert lib.hgo_particles_get(self.h, st.ctypes.data, it.ctypes.data, kl.ctypes.data) == 0
+        return st, it, kl
 
     def thermal(self):
         c = np.empty((self.n, self.n, 4))
