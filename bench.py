@@ -336,6 +336,112 @@ def bench_batch(H, torch, count=64, nsteps=50, warmup=16):
     return out
 
 
+def bench_particles(H, torch, n=1024, count=262144, nsteps=200, warmup=10, cpu_budget_s=6.0):
+    """Droplet erosion (the reference's "particle" erosion type and default
+    particle_count 262144) on a 1024^2 two-layer world from the reference's
+    terrain generator with its particle defaults; the float oracle's
+    sequential restatement times a few steps of the same world on the host."""
+    w = H.World(n, layers=2)
+    ms = H.map_settings(hmap_dims=(n, n))
+    w.init_reference_heightmap(ms)
+    w.particles_init(count)
+    s = H.settings_particles()
+    w.set_erosion(s)
+    w.set_options(H.options(H.RAIN_UNIFORM, seed=11))
+    rock0, dirt0 = w.download("rock"), w.download("dirt")
+    w.step(warmup, H.MODE_PARTICLES)
+    w.sync()
+    torch.cuda.synchronize()
+    l0 = H.lib.hg_launch_count()
+    t0 = time.perf_counter()
+    w.step(nsteps, H.MODE_PARTICLES)
+    w.sync()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    launches = H.lib.hg_launch_count() - l0
+    w.close()
+    out = {"workload": f"{n}x{n} two-layer world (reference terrain), {count} droplets, particle defaults, "
+                       "thermal both layers + smoothing", "steps": nsteps,
+           "droplet_steps_per_s": count * nsteps / el, "ms_per_step": 1e3 * el / nsteps,
+           "launches_per_step": launches / nsteps}
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    ow = O.OracleWorld(n, 32)
+    ow.set("rock", rock0)
+    ow.set("dirt", dirt0)
+    ow.particles_init(count)
+    os_, oo = O.erosion_from(s), O.options(1, 1, 0.0, seed=11)
+    ow.particle_step(os_, oo, 1)
+    k, t0 = 0, time.perf_counter()
+    while True:
+        ow.particle_step(os_, oo, 1)
+        k += 1
+        if time.perf_counter() - t0 >= cpu_budget_s and k >= 2:
+            break
+    cel = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": count * k / cel, "unit": "droplet-steps/s", "cores": O.num_threads(),
+                           "kind": "port", "sample": f"same world, {k} steps in {cel:.1f} s (droplets in id "
+                           "order on one core, grid passes OpenMP)"}
+    return out
+
+
+def bench_render(H, torch, n=1024, width=1920, height=1080, frames=20, cpu_budget_s=6.0):
+    """The headless ray-marcher on a 1024^2 two-layer world from the
+    reference's terrain generator with a lake (water filled to height 96, the
+    reference's WATER_HEIGHT), 1920x1080 from inside the map over the lake; the
+    float oracle renders a 192x108 image of the same view on the host."""
+    w = H.World(n, layers=2)
+    ms = H.map_settings(hmap_dims=(n, n))
+    w.init_reference_heightmap(ms)
+    rock, dirt = w.download("rock"), w.download("dirt")
+    ground = rock + dirt
+    w.upload("water", np.where(ground < 96.0, 96.0 - ground, 0.0).astype(np.float32))
+    cam = H.camera((150.0, 170.0, 150.0), (1.0, -0.35, 1.0), aspect=width / height)
+    img = torch.empty(width * height * 4, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.ExternalStream(w.stream)
+
+    def frame():
+        H.check(H.lib.hg_render_device(w.h, H.ctypes.byref(cam), width, height, img.data_ptr(), None))
+
+    for _ in range(3):
+        frame()
+    w.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(frames):
+        frame()
+    e1.record(stream)
+    e1.synchronize()
+    dev_ms = e0.elapsed_time(e1) / frames
+    host = np.empty((height, width, 4), np.uint8)
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        H.check(H.lib.hg_render(w.h, H.ctypes.byref(cam), width, height, host.ctypes.data, None))
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / frames
+    fields = {k: w.download(k) for k in ("rock", "dirt", "water", "sediment", "sediment_dirt")}
+    w.close()
+    mpix = width * height / 1e6
+    out = {"workload": f"{width}x{height} frame of a {n}x{n} two-layer world with a lake", "frames": frames,
+           "ms_per_frame": dev_ms, "mpixels_per_s": mpix / (dev_ms / 1e3),
+           "e2e": {"ms_per_frame": e2e_ms, "mpixels_per_s": mpix / (e2e_ms / 1e3),
+                   "d2h_bytes_per_frame": width * height * 4},
+           }
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cw, ch = width // 10, height // 10
+    k, t0 = 0, time.perf_counter()
+    while True:
+        O.render(fields, n, cam, cw, ch, ms.max_height, n)
+        k += 1
+        if time.perf_counter() - t0 >= cpu_budget_s:
+            break
+    cel = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": k * cw * ch / 1e6 / cel, "unit": "Mpixel/s", "cores": O.num_threads(),
+                           "kind": "port", "sample": f"{cw}x{ch} image of the same view, {k} frames in {cel:.1f} s "
+                           "(float oracle, OpenMP over rows)"}
+    return out
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -472,6 +578,8 @@ def main():
         line["fwd_adjoint"] = bench_adjoint(H, torch)
         line["batch"] = bench_batch(H, torch)
         line["large"] = bench_large(H, torch)
+        line["particles"] = bench_particles(H, torch)
+        line["render"] = bench_render(H, torch)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)

@@ -57,6 +57,25 @@ void launch_thermal_out1(const StepConsts& c, const float* rock, const float* di
 void launch_smooth2(const StepConsts& c, const float* rock, const float* dirt, float* rock_o, float* dirt_o,
                     cudaStream_t st);
 
+// ---- headless ray-marcher (hg_render.cu) ------------------------------------------
+struct RenderInput {
+    int n;
+    float max_height;  // map settings: the shadow rays' ceiling
+    int hmap_dim_x;    // map settings: alpha of the low-resolution form
+    const float* rock;
+    const float* dirt;   // nullptr: one-layer world
+    const float* water;
+    const float* sed0;
+    const float* sed1;   // nullptr: one-layer world
+    float4* hm;          // n*n packed heightmap texels (written)
+    float2* sed;         // n*n packed sediment texels (written when displayed)
+};
+// packs the heightmap and renders width x height pixels into rgba_dev
+// (and the float colour into rgb_dev when not null); HG_ERR_INVALID for a
+// singular view or perspective matrix
+int render_image(const RenderInput& in, const hg_camera& cam, int width, int height, uint8_t* rgba_dev,
+                 float* rgb_dev, cudaStream_t st);
+
 // ---- particle erosion (hg_particles.cu) --------------------------------------------
 // Droplets as structure of arrays (Particle, glsl/bindings.glsl:101-110).
 struct Drops {

@@ -113,6 +113,11 @@ struct hg_world {
     float* red_f = nullptr;   // min/max partials + result
     double* red_d = nullptr;  // FP64 partials + result
     hg::Particles* parts = nullptr;  // particle mode: droplets and momentum map
+    float4* r_hm = nullptr;          // ray-marcher: packed heightmap texels
+    float2* r_sed = nullptr;         // ray-marcher: packed sediment texels
+    uint8_t* r_rgba = nullptr;       // hg_render: device image
+    float* r_rgb = nullptr;
+    size_t r_pixels = 0;             // capacity of r_rgba / r_rgb
 };
 
 struct hg_batch {
@@ -212,6 +217,7 @@ void free_world(hg_world* w) {
     cudaFree(w->red_f); cudaFree(w->red_d);
     delete w->parts;
     w->parts = nullptr;
+    cudaFree(w->r_hm); cudaFree(w->r_sed); cudaFree(w->r_rgba); cudaFree(w->r_rgb);
     if (w->stream) cudaStreamDestroy(w->stream);
 }
 
@@ -898,6 +904,95 @@ int hg_init_reference_heightmap(hg_world* w, const hg_map_settings* s) {
     w->version += 1;
     w->step = 0;
     w->dev_step_valid = false;
+    return HG_OK;
+}
+
+int hg_camera_look_at(hg_camera* out, const float pos[3], const float dir[3], const float up[3], float fov_deg,
+                      float aspect, float z_near, float z_far) {
+    if (!out || !pos || !dir || !up) return fail(HG_ERR_INVALID, "null argument");
+    if (!(aspect > 0.0f) || !(z_far > z_near) || !(fov_deg > 0.0f && fov_deg < 180.0f))
+        return fail(HG_ERR_INVALID, "bad projection");
+    std::memset(out, 0, sizeof(*out));
+    auto norm = [](float v[3]) {
+        const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        v[0] /= l; v[1] /= l; v[2] /= l;
+    };
+    auto cross = [](const float a[3], const float b[3], float r[3]) {
+        r[0] = a[1] * b[2] - b[1] * a[2];
+        r[1] = a[2] * b[0] - b[2] * a[0];
+        r[2] = a[0] * b[1] - b[0] * a[1];
+    };
+    auto dot = [](const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    // lookAt(eye = pos, center = pos + dir, up), right-handed
+    float f[3] = {(pos[0] + dir[0]) - pos[0], (pos[1] + dir[1]) - pos[1], (pos[2] + dir[2]) - pos[2]};
+    norm(f);
+    float s[3], u[3];
+    cross(f, up, s);
+    norm(s);
+    cross(s, f, u);
+    float* V = out->view;
+    V[0] = s[0]; V[4] = s[1]; V[8] = s[2];
+    V[1] = u[0]; V[5] = u[1]; V[9] = u[2];
+    V[2] = -f[0]; V[6] = -f[1]; V[10] = -f[2];
+    V[12] = -dot(s, pos); V[13] = -dot(u, pos); V[14] = dot(f, pos);
+    V[15] = 1.0f;
+    // perspective, depth -1..1
+    const float th = std::tan(fov_deg * 0.01745329251994329577f / 2.0f);
+    float* P = out->perspective;
+    P[0] = 1.0f / (aspect * th);
+    P[5] = 1.0f / th;
+    P[10] = -(z_far + z_near) / (z_far - z_near);
+    P[11] = -1.0f;
+    P[14] = -(2.0f * z_far * z_near) / (z_far - z_near);
+    for (int k = 0; k < 3; ++k) out->pos[k] = pos[k];
+    out->prec = 0.35f;
+    out->draw_water = 1;
+    out->display_sediment = 0;
+    out->sediment_max_cap = 0.1f;
+    out->low_res_div3 = 0;
+    return HG_OK;
+}
+
+int hg_render_device(hg_world* w, const hg_camera* cam, int width, int height, uint8_t* rgba_dev, float* rgb_dev) {
+    HG_CHECK_WORLD(w);
+    if (!cam || !rgba_dev) return fail(HG_ERR_INVALID, "null argument");
+    if (width < 1 || height < 1 || (size_t)width * height > (size_t)1 << 28)
+        return fail(HG_ERR_INVALID, "image size must be in [1, 2^28] pixels");
+    if (!(cam->prec > 0.0f) || !std::isfinite(cam->prec)) return fail(HG_ERR_INVALID, "prec must be positive");
+    DeviceGuard g(w->device);
+    const size_t bytes = cells(w);
+    if (!w->r_hm) HG_CUDA(cudaMalloc((void**)&w->r_hm, bytes * sizeof(float4)));
+    if (cam->display_sediment && !w->r_sed) HG_CUDA(cudaMalloc((void**)&w->r_sed, bytes * sizeof(float2)));
+    RenderInput in{w->n, w->map.max_height, w->map.hmap_dims[0], w->cur[S_ROCK], w->layers == 2 ? w->dirt[0] : nullptr,
+                   w->cur[S_WATER], w->cur[S_SED], w->layers == 2 ? w->sdirt[0] : nullptr, w->r_hm, w->r_sed};
+    int rc = render_image(in, *cam, width, height, rgba_dev, rgb_dev, w->stream);
+    if (rc != HG_OK) return fail(rc, "singular view or perspective matrix");
+    HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+
+int hg_render(hg_world* w, const hg_camera* cam, int width, int height, uint8_t* rgba, float* rgb) {
+    HG_CHECK_WORLD(w);
+    if (!cam || !rgba) return fail(HG_ERR_INVALID, "null argument");
+    if (width < 1 || height < 1 || (size_t)width * height > (size_t)1 << 28)
+        return fail(HG_ERR_INVALID, "image size must be in [1, 2^28] pixels");
+    DeviceGuard g(w->device);
+    const size_t px = (size_t)width * height;
+    if (px > w->r_pixels) {
+        cudaFree(w->r_rgba);
+        cudaFree(w->r_rgb);
+        w->r_rgba = nullptr;
+        w->r_rgb = nullptr;
+        w->r_pixels = 0;
+        HG_CUDA(cudaMalloc((void**)&w->r_rgba, px * 4));
+        HG_CUDA(cudaMalloc((void**)&w->r_rgb, px * 3 * sizeof(float)));
+        w->r_pixels = px;
+    }
+    int rc = hg_render_device(w, cam, width, height, w->r_rgba, rgb ? w->r_rgb : nullptr);
+    if (rc != HG_OK) return rc;
+    HG_CUDA(cudaMemcpyAsync(rgba, w->r_rgba, px * 4, cudaMemcpyDeviceToHost, w->stream));
+    if (rgb) HG_CUDA(cudaMemcpyAsync(rgb, w->r_rgb, px * 3 * sizeof(float), cudaMemcpyDeviceToHost, w->stream));
+    HG_CUDA(cudaStreamSynchronize(w->stream));
     return HG_OK;
 }
 

@@ -33,6 +33,13 @@ FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_
 STATE_FIELDS = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"]
 
 
+class Camera(ctypes.Structure):
+    """hg_camera: the ray-marcher's uniforms (glsl/rendering.glsl:15-23)."""
+    _fields_ = [("view", ctypes.c_float * 16), ("perspective", ctypes.c_float * 16), ("pos", ctypes.c_float * 3),
+                ("prec", ctypes.c_float), ("draw_water", ctypes.c_int32), ("display_sediment", ctypes.c_int32),
+                ("sediment_max_cap", ctypes.c_float), ("low_res_div3", ctypes.c_int32)]
+
+
 class HydrogenError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"{STATUS.get(code, code)}: {msg}")
@@ -125,6 +132,10 @@ def _load():
         "hg_set_map_settings": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
         "hg_init_reference_heightmap": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
         "hg_particles_init": (ctypes.c_int, [P, ctypes.c_int]),
+        "hg_camera_look_at": (ctypes.c_int, [ctypes.POINTER(Camera), P, P, P, ctypes.c_float, ctypes.c_float,
+                                             ctypes.c_float, ctypes.c_float]),
+        "hg_render": (ctypes.c_int, [P, ctypes.POINTER(Camera), ctypes.c_int, ctypes.c_int, P, P]),
+        "hg_render_device": (ctypes.c_int, [P, ctypes.POINTER(Camera), ctypes.c_int, ctypes.c_int, P, P]),
         "hg_default_particle_settings": (ctypes.c_int, [ctypes.POINTER(ErosionSettings)]),
         "hg_particles_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
         "hg_particles_get": (ctypes.c_int, [P, P, P, P]),
@@ -198,6 +209,23 @@ def settings_particles():
     s = ErosionSettings()
     check(lib.hg_default_particle_settings(ctypes.byref(s)))
     return s
+
+
+def camera(pos, dir, up=(0.0, 1.0, 0.0), fov=90.0, aspect=16.0 / 9.0, z_near=0.1, z_far=2048.0):
+    """hg_camera of glm::lookAt(pos, pos + dir, up) and glm::perspective
+    (src/rendering.cpp:89-99; FOV 90, Z_NEAR 0.1, Z_FAR 2048)."""
+    c = Camera()
+    f3 = ctypes.c_float * 3
+    check(lib.hg_camera_look_at(ctypes.byref(c), f3(*pos), f3(*dir), f3(*up), fov, aspect, z_near, z_far))
+    return c
+
+
+def save_ppm(path, rgba):
+    """Writes an RGBA8 image (row 0 = bottom, as rendered) as a binary PPM."""
+    img = np.ascontiguousarray(rgba[::-1, :, :3])
+    with open(path, "wb") as f:
+        f.write(f"P6 {img.shape[1]} {img.shape[0]} 255\n".encode())
+        f.write(img.tobytes())
 
 
 def rain_uniform(amount=0.01, period=1):
@@ -291,6 +319,15 @@ class World:
 
     def set_map(self, ms):
         check(lib.hg_set_map_settings(self.h, ctypes.byref(ms)))
+
+    def render(self, cam, width, height, rgb=False):
+        """Ray-marched image: rgba[h, w, 4] uint8 (row 0 = bottom), and the
+        float colour rgb[h, w, 3] when asked."""
+        img = np.empty((height, width, 4), np.uint8)
+        col = np.empty((height, width, 3), np.float32) if rgb else None
+        check(lib.hg_render(self.h, ctypes.byref(cam), width, height, img.ctypes.data,
+                            col.ctypes.data if rgb else None))
+        return (img, col) if rgb else img
 
     def particles_init(self, count):
         """`count` idle droplets and a zero momentum map (two-layer worlds)."""

@@ -235,6 +235,36 @@ int hg_particles_count(const hg_world* w, int* count);
  * capacity), iters the age in steps (0: idle), kill 1 for a droplet that
  * respawns on the next step. */
 int hg_particles_get(hg_world* w, float* state8, uint32_t* iters, int32_t* kill);
+/* Camera of the headless ray-marcher: the uniforms of glsl/rendering.glsl:15-23
+ * that Render::Data::dispatch sets (src/rendering.cpp:79-140).  Matrices
+ * are column-major as glm stores them. */
+typedef struct hg_camera {
+    float view[16];          /* glm::lookAt(pos, pos + dir, up) */
+    float perspective[16];   /* glm::perspective(radians(FOV), aspect, Z_NEAR, Z_FAR) */
+    float pos[3];            /* ray origin (uniform pos) */
+    float prec;              /* march step factor (0.35; UI range 0.01..1) */
+    int32_t draw_water;      /* should_draw_water (1) */
+    int32_t display_sediment;/* tint by suspended sediment (0) */
+    float sediment_max_cap;  /* sediment giving full tint (0.1) */
+    int32_t low_res_div3;    /* the LOW_RES_DIV3 build: march width/3 x height/3
+                                pixels, each stored as a 3x3 block */
+} hg_camera;
+
+/* Fills view and perspective as src/rendering.cpp:89-99 does (glm's
+ * right-handed lookAt and perspective with depth -1..1) and the other fields
+ * with the shader's defaults.  FOV 90, Z_NEAR 0.1, Z_FAR 2048 are the
+ * reference's (src/rendering.hpp:11-13). */
+int hg_camera_look_at(hg_camera* out, const float pos[3], const float dir[3], const float up[3], float fov_deg,
+                      float aspect, float z_near, float z_far);
+/* Renders the world into width x height RGBA8 pixels (row y = 0 first, the
+ * GL image's bottom row; alpha 0, or 255 in the low-resolution form) and,
+ * if rgb is not NULL, the gamma-corrected float colour (3 floats per pixel).
+ * hg_render copies into host memory and waits; hg_render_device writes
+ * device memory in the world's stream order.  The shader's pow and exp use
+ * the library's own exp2 / log2 (GLSL leaves their precision to the driver),
+ * so a render is reproducible bit for bit. */
+int hg_render(hg_world* w, const hg_camera* cam, int width, int height, uint8_t* rgba, float* rgb);
+int hg_render_device(hg_world* w, const hg_camera* cam, int width, int height, uint8_t* rgba_dev, float* rgb_dev);
 /* Replaces State::World::delete_textures (src/state.cpp:46-55). */
 int hg_world_destroy(hg_world* w);
 int hg_world_size(const hg_world* w, int* n);

@@ -317,6 +317,53 @@ def ref_noised(x, y):
     return tuple(out)
 
 
+lib.hgo_render.restype = ctypes.c_int
+lib.hgo_render.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_void_p,
+                                                   ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+for _f in ("hgo_render_pow",):
+    getattr(lib, _f).restype = ctypes.c_float
+    getattr(lib, _f).argtypes = [ctypes.c_float, ctypes.c_float]
+for _f in ("hgo_render_exp2", "hgo_render_log2"):
+    getattr(lib, _f).restype = ctypes.c_float
+    getattr(lib, _f).argtypes = [ctypes.c_float]
+
+
+def render(fields, n, camera, width, height, max_height=256.0, hmap_dim_x=1024):
+    """The ray-marcher (glsl/rendering.glsl) on host fields: dict with rock,
+    water, sediment and, for two-layer worlds, dirt and sediment_dirt;
+    camera any ctypes struct with hg_camera's layout.  Returns (rgba[h, w, 4]
+    uint8, rgb[h, w, 3] float32), row 0 first."""
+    keep = []
+
+    def ptr(name):
+        if name not in fields:
+            return None
+        a = np.ascontiguousarray(fields[name], dtype=np.float32)
+        assert a.size == n * n
+        keep.append(a)
+        return a.ctypes.data
+
+    rgba = np.zeros((height, width, 4), np.uint8)
+    rgb = np.zeros((height, width, 3), np.float32)
+    rc = lib.hgo_render(ptr("rock"), ptr("dirt"), ptr("water"), ptr("sediment"), ptr("sediment_dirt"), n,
+                        max_height, hmap_dim_x, ctypes.byref(camera), width, height, rgba.ctypes.data,
+                        rgb.ctypes.data)
+    assert rc == 0, "singular camera matrices"
+    return rgba, rgb
+
+
+def render_pow(x, y):
+    return lib.hgo_render_pow(x, y)
+
+
+def render_exp2(x):
+    return lib.hgo_render_exp2(x)
+
+
+def render_log2(x):
+    return lib.hgo_render_log2(x)
+
+
 def _adj_settings(s, amount):
     return np.array([s.d_t, s.G, s.ENERGY_KEPT, s.Kc, s.Kd[0], s.Ke, amount, s.Kalpha[0], s.Kspeed[0]],
                     dtype=np.float32)
