@@ -260,11 +260,50 @@ __device__ __forceinline__ void outflows_scalar(const StepConsts& c, const float
     cell_thermal_outflows(c, b, nb, o8);
 }
 
+// Talus outflows of the row group of four cells at region (rx0, ry), global
+// (x0, y), from the staged eroded rock; a row outside the grid has none.
+template <bool EDGE>
+__device__ __forceinline__ void group_outflows(const StepConsts& c, const float* be, int rx0, int ry, int x0, int y,
+                                               float o[8][4]) {
+    const int n = c.n;
+    if (EDGE && (y < 0 || y >= n)) {
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) o[d][j] = 0.0f;
+        return;
+    }
+    const int si = ry * RW + rx0;
+    const float4 m4 = ld4(be + si - RW), c4 = ld4(be + si), p4 = ld4(be + si + RW);
+    const float ml = be[si - RW - 1], mr = be[si - RW + 4];
+    const float cl = be[si - 1], cr = be[si + 4];
+    const float pl = be[si + RW - 1], pr = be[si + RW + 4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int x = x0 + j;
+        const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
+        const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
+        float nb[8];
+        nb[0] = has_l ? (j == 0 ? cl : at4(c4, j - 1)) : FAR_HEIGHT;
+        nb[1] = has_r ? (j == 3 ? cr : at4(c4, j + 1)) : FAR_HEIGHT;
+        nb[2] = has_t ? at4(p4, j) : FAR_HEIGHT;
+        nb[3] = has_b ? at4(m4, j) : FAR_HEIGHT;
+        nb[4] = (has_l && has_t) ? (j == 0 ? pl : at4(p4, j - 1)) : FAR_HEIGHT;
+        nb[5] = (has_r && has_t) ? (j == 3 ? pr : at4(p4, j + 1)) : FAR_HEIGHT;
+        nb[6] = (has_l && has_b) ? (j == 0 ? ml : at4(m4, j - 1)) : FAR_HEIGHT;
+        nb[7] = (has_r && has_b) ? (j == 3 ? mr : at4(m4, j + 1)) : FAR_HEIGHT;
+        float o8[8];
+        cell_thermal_outflows(c, at4(c4, j), nb, o8);
+#pragma unroll
+        for (int d = 0; d < 8; ++d) o[d][j] = o8[d];
+    }
+}
+
 template <int TH, bool EDGE>
 __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUtensorMap* maps, float* be, float* outf,
                                                uint64_t* bar, int tx0, int ty0, int* err) {
     using G = Geo<TH>;
-    constexpr int NTH = G::NTH, O_C = G::O_C;
+    constexpr int O_C = G::O_C;
     const StepConsts& c = td.c;
     const int n = c.n;
     const int tid = threadIdx.x;
@@ -303,41 +342,27 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
         return;
     }
     // ---- outflows of the interior row groups (one per thread) --------------
+    // The thread's own outflow sums (cell_thermal_apply's sum = 0 - own[0] -
+    // ... - own[7]) stay in registers.
     const int rx0 = HX + 4 * g, ry = 2 + iy;  // region coords of the group's first cell
+    const int oi = (ry - 1) * RW + rx0;
+    float osum[4];
     {
-        const int si = ry * RW + rx0;
-        const float4 m4 = ld4(be + si - RW), c4 = ld4(be + si), p4 = ld4(be + si + RW);
-        const float ml = be[si - RW - 1], mr = be[si - RW + 4];
-        const float cl = be[si - 1], cr = be[si + 4];
-        const float pl = be[si + RW - 1], pr = be[si + RW + 4];
         float o[8][4];
+        group_outflows<EDGE>(c, be, rx0, ry, x0, y, o);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int x = x0 + j;
-            const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
-            const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
-            float nb[8];
-            nb[0] = has_l ? (j == 0 ? cl : at4(c4, j - 1)) : FAR_HEIGHT;
-            nb[1] = has_r ? (j == 3 ? cr : at4(c4, j + 1)) : FAR_HEIGHT;
-            nb[2] = has_t ? at4(p4, j) : FAR_HEIGHT;
-            nb[3] = has_b ? at4(m4, j) : FAR_HEIGHT;
-            nb[4] = (has_l && has_t) ? (j == 0 ? pl : at4(p4, j - 1)) : FAR_HEIGHT;
-            nb[5] = (has_r && has_t) ? (j == 3 ? pr : at4(p4, j + 1)) : FAR_HEIGHT;
-            nb[6] = (has_l && has_b) ? (j == 0 ? ml : at4(m4, j - 1)) : FAR_HEIGHT;
-            nb[7] = (has_r && has_b) ? (j == 3 ? mr : at4(m4, j + 1)) : FAR_HEIGHT;
-            float o8[8];
-            cell_thermal_outflows(c, at4(c4, j), nb, o8);
+            osum[j] = 0.0f;
 #pragma unroll
-            for (int d = 0; d < 8; ++d) o[d][j] = o8[d];
+            for (int d = 0; d < 8; ++d) osum[j] -= o[d][j];
         }
-        const int oi = (ry - 1) * RW + rx0;
 #pragma unroll
         for (int d = 0; d < 8; ++d) st4(outf + d * O_C + oi, make_float4(o[d][0], o[d][1], o[d][2], o[d][3]));
     }
     // ---- outflows of the ring of interior plus 1 ---------------------------
     {
         constexpr int RING = 2 * TW + 2 * (TH + 2);
-        for (int q = tid; q < RING; q += NTH) {
+        for (int q = tid; q < RING; q += G::NTH) {
             int rx, ry2;
             if (q < TW) { rx = HX + q; ry2 = 1; }
             else if (q < 2 * TW) { rx = HX + q - TW; ry2 = TH + 2; }
@@ -345,9 +370,9 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
             else { rx = HX + TW; ry2 = 1 + q - 2 * TW - (TH + 2); }
             float o8[8];
             outflows_scalar<EDGE>(c, be, rx, ry2, gx0 + rx, gy0 + ry2, o8);
-            const int oi = (ry2 - 1) * RW + rx;
+            const int ro = (ry2 - 1) * RW + rx;
 #pragma unroll
-            for (int d = 0; d < 8; ++d) outf[d * O_C + oi] = o8[d];
+            for (int d = 0; d < 8; ++d) outf[d * O_C + ro] = o8[d];
         }
     }
     __syncthreads();
@@ -355,21 +380,7 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
     // (cell_thermal_apply's operations: in_flux = in[0] + ... + in[7] from 0,
     // sum = 0 - own[0] - ... - own[7], rock = b + (sum + in_flux))
     {
-        const int oi = (ry - 1) * RW + rx0;
         const float4 oL = ld4(outf + 0 * O_C + oi), oR = ld4(outf + 1 * O_C + oi);
-        float osum[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            osum[j] = 0.0f;
-            osum[j] -= at4(oL, j);
-            osum[j] -= at4(oR, j);
-        }
-#pragma unroll
-        for (int d = 2; d < 8; ++d) {
-            const float4 o = ld4(outf + d * O_C + oi);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) osum[j] -= at4(o, j);
-        }
         // inflow from direction d = neighbour (dx, dy)'s outflow toward this
         // cell.  Rows of outflows are read as aligned float4 (the group's own
         // four columns); the column left (right) of the group comes from the

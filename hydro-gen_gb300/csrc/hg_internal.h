@@ -94,6 +94,9 @@ struct ParticleBufs {
     uint32_t* cursor;      // n*n scatter cursors
     uint32_t* block_sums;  // particle_scan_blocks(n*n)
     uint32_t* keys;        // 4*count records (droplet * 4 + corner), bucketed by texel
+    uint32_t* sorted;      // 4*count: hot texels' buckets in droplet-id order
+    uint32_t* hot;         // 1 + hot_cap: count of hot texels, then their indices
+    uint32_t hot_cap;      // particle_hot_capacity(n*n, count)
     float* rec;            // 8*count: per record the dirt and rock sediment it left
     uint8_t* rec_mask;     // 4*count: which layers a record set
 };
@@ -105,6 +108,7 @@ struct PWorld {
     float* mom[4];
 };
 size_t particle_scan_blocks(size_t cells);
+size_t particle_hot_capacity(size_t cells, int count);
 // movement, counting sort, erosion in droplet-id order, sediment replay
 void launch_particle_step(const StepConsts& c, const hg_erosion_settings& es, const ParticleBufs& pb,
                           const PWorld& pw, uint32_t step1, uint64_t seed, bool should_rain, cudaStream_t st);

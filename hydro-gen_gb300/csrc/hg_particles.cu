@@ -8,17 +8,21 @@
 // no thread waits on another:
 //   k_pcount / scan / k_pscatter   counting sort of the droplets' four corner
 //                                  records by texel
-//   k_papply                       each texel applies its records in
+//   k_papply / k_papply_hot        each texel applies its records in
 //                                  droplet-id order (a texel update needs only
 //                                  the droplet's state from before the pass)
 //                                  and stores what each corner left for the
-//                                  droplet's sediment
+//                                  droplet's sediment; a texel with up to 8
+//                                  records sorts them in registers, busier
+//                                  ones get a warp each
 //   k_pfinal                       each droplet replays its corners 0..3
 // which is a sequential pass over droplets in id order, corners in order.
 // Spawn positions come from Philox4x32-10 (counter: droplet id, step,
 // 'part', 0; key: the rain seed), 24-bit uniforms; the shader's
 // fract(1e4 sin(...)) hash of the frame time has no portable bits.
 #include "hg_internal.h"
+
+#include <algorithm>
 
 namespace hg {
 
@@ -250,7 +254,10 @@ struct ApplyArgs {
     Drops d;
     int n;
     const uint32_t* offs;  // n*n + 1
-    uint32_t* keys;
+    const uint32_t* keys;  // records bucketed by texel, any order within a bucket
+    uint32_t* sorted;      // hot texels: their bucket in droplet-id order
+    uint32_t* hot;         // [0]: hot texel count, then the hot texels
+    uint32_t hot_cap;
     float* rock;
     float* dirt;
     float* water;
@@ -260,7 +267,92 @@ struct ApplyArgs {
     uint8_t* rec_mask;     // bit 1: dirt layer handled, bit 0: rock layer handled
 };
 
-// each texel applies its records in droplet-id order
+// A record's inputs: all from before the pass
+struct Rec {
+    uint32_t key;
+    float multipl, sc, vol, s0, s1, vx, vy;
+    int kill;
+};
+
+__device__ __forceinline__ Rec load_rec(const ApplyArgs& a, uint32_t key) {
+    Rec r;
+    r.key = key;
+    const int id = (int)(key >> 2), k = (int)(key & 3u);
+    int cx, cy;
+    corner(a.d.px[id], a.d.py[id], k, a.n, cx, cy, r.multipl);
+    r.sc = a.d.sc[id];
+    r.vol = a.d.vol[id];
+    r.s0 = a.d.s0[id];
+    r.s1 = a.d.s1[id];
+    r.vx = a.d.vx[id];
+    r.vy = a.d.vy[id];
+    r.kill = a.d.kill[id];
+    return r;
+}
+
+struct Texel {
+    float terr[2], wat, mz, mw;
+};
+
+// one droplet corner on its texel (glsl/particle_erosion.glsl:66-122): the
+// layer loop from dirt down to rock, then water and momentum
+__device__ __forceinline__ void apply_record(const ApplyArgs& a, const Rec& r, Texel& T) {
+    const float old_sed[2] = {r.s0, r.s1};
+    float s_out[2] = {0.0f, 0.0f};
+    uint32_t mask = 0;
+    float cap = 0.0f;
+    for (int l = 1; l >= 0; --l) {
+        if (r.kill) {
+            T.terr[l] += old_sed[l] * r.multipl;
+            continue;
+        }
+        const float Kls = a.es.d_t * a.es.Ks[l], Kld = a.es.d_t * a.es.Kd[l];
+        const float c = gmax(0.0f, r.sc - cap);
+        float s1 = old_sed[l];
+        const float old_terr = T.terr[l];
+        mask |= 1u << l;
+        if (c > s1) {
+            const float eroded = r.multipl * Kls * (c - s1);
+            s1 += eroded;
+            T.terr[l] -= eroded;
+            if (T.terr[l] < 0.0f) {
+                s1 += T.terr[l];
+                T.terr[l] = 0.0f;
+                cap += old_terr;
+            } else {
+                s_out[l] = s1;
+                break;
+            }
+        } else {
+            const float deposit = r.multipl * Kld * (s1 - c);
+            s1 -= deposit;
+            T.terr[l] += deposit;
+        }
+        s_out[l] = s1;
+    }
+    a.rec[2 * r.key + 0] = s_out[1];
+    a.rec[2 * r.key + 1] = s_out[0];
+    a.rec_mask[r.key] = (uint8_t)mask;
+    T.wat += 1e-5f * r.vol * r.multipl;
+    T.mz += r.vol * r.vx * r.multipl;
+    T.mw += r.vol * r.vy * r.multipl;
+}
+
+__device__ __forceinline__ Texel load_texel(const ApplyArgs& a, size_t t) {
+    return Texel{{a.rock[t], a.dirt[t]}, a.water[t], a.mz[t], a.mw[t]};
+}
+__device__ __forceinline__ void store_texel(const ApplyArgs& a, size_t t, const Texel& T) {
+    a.rock[t] = T.terr[0];
+    a.dirt[t] = T.terr[1];
+    a.water[t] = T.wat;
+    a.mz[t] = T.mz;
+    a.mw[t] = T.mw;
+}
+
+constexpr int SMALL = 8;  // records a texel's own thread sorts and applies
+
+// each texel with at most SMALL records applies them in droplet-id order;
+// busier texels go to the hot list
 __global__ void k_papply(const ApplyArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = a.n;
@@ -268,70 +360,85 @@ __global__ void k_papply(const ApplyArgs a) {
     const size_t t = (size_t)y * n + x;
     const uint32_t lo = a.offs[t], hi = a.offs[t + 1];
     if (lo == hi) return;
-    for (uint32_t i = lo + 1; i < hi; ++i) {  // insertion sort of the texel's records
-        const uint32_t k = a.keys[i];
-        uint32_t j = i;
-        while (j > lo && a.keys[j - 1] > k) {
-            a.keys[j] = a.keys[j - 1];
-            --j;
-        }
-        a.keys[j] = k;
+    const uint32_t k = hi - lo;
+    if (k > SMALL) {
+        const uint32_t slot = atomicAdd(a.hot, 1u);
+        if (slot < a.hot_cap) a.hot[1 + slot] = (uint32_t)t;
+        return;
     }
-    float terr[2] = {a.rock[t], a.dirt[t]};
-    float wat = a.water[t], mz = a.mz[t], mw = a.mw[t];
-    for (uint32_t i = lo; i < hi; ++i) {
-        const uint32_t key = a.keys[i];
-        const int id = (int)(key >> 2), k = (int)(key & 3u);
-        int cx, cy;
-        float multipl;
-        corner(a.d.px[id], a.d.py[id], k, n, cx, cy, multipl);
-        const float old_sed[2] = {a.d.s0[id], a.d.s1[id]};
-        const bool kill = a.d.kill[id] != 0;
-        const float sc = a.d.sc[id], vol = a.d.vol[id];
-        float s_out[2] = {0.0f, 0.0f};
-        uint32_t mask = 0;
-        float cap = 0.0f;
-        for (int l = 1; l >= 0; --l) {
-            if (kill) {
-                terr[l] += old_sed[l] * multipl;
-                continue;
-            }
-            const float Kls = a.es.d_t * a.es.Ks[l], Kld = a.es.d_t * a.es.Kd[l];
-            const float c = gmax(0.0f, sc - cap);
-            float s1 = old_sed[l];
-            const float old_terr = terr[l];
-            mask |= 1u << l;
-            if (c > s1) {
-                const float eroded = multipl * Kls * (c - s1);
-                s1 += eroded;
-                terr[l] -= eroded;
-                if (terr[l] < 0.0f) {
-                    s1 += terr[l];
-                    terr[l] = 0.0f;
-                    cap += old_terr;
-                } else {
-                    s_out[l] = s1;
-                    break;
+    uint32_t kk[SMALL];
+#pragma unroll
+    for (int i = 0; i < SMALL; ++i) kk[i] = (uint32_t)i < k ? a.keys[lo + i] : 0xffffffffu;
+    // sorting network on registers (odd-even transposition, SMALL rounds)
+#pragma unroll
+    for (int r = 0; r < SMALL; ++r)
+#pragma unroll
+        for (int i = r & 1; i + 1 < SMALL; i += 2) {
+            const uint32_t u = min(kk[i], kk[i + 1]), v = max(kk[i], kk[i + 1]);
+            kk[i] = u;
+            kk[i + 1] = v;
+        }
+    Texel T = load_texel(a, t);
+#pragma unroll
+    for (int i = 0; i < SMALL; ++i)
+        if ((uint32_t)i < k) apply_record(a, load_rec(a, kk[i]), T);
+    store_texel(a, t, T);
+}
+
+constexpr int HOT_WARPS = 4;     // warps per block of k_papply_hot
+constexpr int HOT_KEYS = 2048;   // bucket size a warp sorts in shared memory
+
+// one warp per hot texel: sort the bucket by droplet id (bitonic network in
+// shared memory; buckets above HOT_KEYS by rank counting over global
+// memory), then stage 32 records at a time in shared memory for lane 0's
+// sequential update
+__global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_hot(const ApplyArgs a) {
+    __shared__ uint32_t sk[HOT_WARPS][HOT_KEYS];
+    __shared__ Rec sr[HOT_WARPS][32];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint32_t nhot = min(a.hot[0], a.hot_cap);
+    for (uint32_t h = blockIdx.x * HOT_WARPS + wl; h < nhot; h += gridDim.x * HOT_WARPS) {
+        const size_t t = a.hot[1 + h];
+        const uint32_t lo = a.offs[t], hi = a.offs[t + 1], k = hi - lo;
+        if (k <= (uint32_t)HOT_KEYS) {
+            uint32_t P = 32;
+            while (P < k) P <<= 1;
+            for (uint32_t i = lane; i < P; i += 32) sk[wl][i] = i < k ? a.keys[lo + i] : 0xffffffffu;
+            __syncwarp();
+            for (uint32_t size = 2; size <= P; size <<= 1)
+                for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                    for (uint32_t q = lane; q < P / 2; q += 32) {
+                        const uint32_t pos = 2 * stride * (q / stride) + (q % stride), par = pos + stride;
+                        const bool up = (pos & size) == 0;
+                        const uint32_t u = sk[wl][pos], v = sk[wl][par];
+                        if ((u > v) == up) {
+                            sk[wl][pos] = v;
+                            sk[wl][par] = u;
+                        }
+                    }
+                    __syncwarp();
                 }
-            } else {
-                const float deposit = multipl * Kld * (s1 - c);
-                s1 -= deposit;
-                terr[l] += deposit;
+            for (uint32_t i = lane; i < k; i += 32) a.sorted[lo + i] = sk[wl][i];
+        } else {
+            for (uint32_t i = lane; i < k; i += 32) {
+                const uint32_t key = a.keys[lo + i];
+                uint32_t rank = 0;
+                for (uint32_t j = 0; j < k; ++j) rank += a.keys[lo + j] < key ? 1u : 0u;
+                a.sorted[lo + rank] = key;
             }
-            s_out[l] = s1;
         }
-        a.rec[2 * key + 0] = s_out[1];
-        a.rec[2 * key + 1] = s_out[0];
-        a.rec_mask[key] = (uint8_t)mask;
-        wat += 1e-5f * vol * multipl;
-        mz += vol * a.d.vx[id] * multipl;
-        mw += vol * a.d.vy[id] * multipl;
+        __syncwarp();
+        Texel T = load_texel(a, t);
+        for (uint32_t base = lo; base < hi; base += 32) {
+            const uint32_t m = min(32u, hi - base);
+            if ((uint32_t)lane < m) sr[wl][lane] = load_rec(a, a.sorted[base + lane]);
+            __syncwarp();
+            if (lane == 0)
+                for (uint32_t i = 0; i < m; ++i) apply_record(a, sr[wl][i], T);
+            __syncwarp();
+        }
+        if (lane == 0) store_texel(a, t, T);
     }
-    a.rock[t] = terr[0];
-    a.dirt[t] = terr[1];
-    a.water[t] = wat;
-    a.mz[t] = mz;
-    a.mw[t] = mw;
 }
 
 // each droplet replays its corners 0..3 for its sediment
@@ -413,6 +520,9 @@ __global__ void k_psmooth(const SmoothArgs a) {
 }  // namespace
 
 size_t particle_scan_blocks(size_t cells) { return (cells + SCAN_T * SCAN_E - 1) / (SCAN_T * SCAN_E); }
+size_t particle_hot_capacity(size_t cells, int count) {
+    return std::min(cells, (size_t)4 * (size_t)count / (SMALL + 1) + 1);
+}
 
 void launch_particle_step(const StepConsts& c, const hg_erosion_settings& es, const ParticleBufs& pb,
                           const PWorld& pw, uint32_t step1, uint64_t seed, bool should_rain, cudaStream_t st) {
@@ -429,11 +539,14 @@ void launch_particle_step(const StepConsts& c, const hg_erosion_settings& es, co
     k_scan_sums<<<1, SCAN_T, 0, st>>>(pb.block_sums, (int)nb, pb.offs + cells);
     k_scan_add<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(pb.offs, pb.cursor, cells, pb.block_sums);
     k_pscatter<<<pgrid, PB, 0, st>>>(pb.d, n, pb.cursor, pb.keys);
-    ApplyArgs aa{es, pb.d, n, pb.offs, pb.keys, pw.rock, pw.dirt, pw.water, pw.mom[2], pw.mom[3], pb.rec, pb.rec_mask};
+    ApplyArgs aa{es, pb.d, n, pb.offs, pb.keys, pb.sorted, pb.hot, pb.hot_cap, pw.rock, pw.dirt, pw.water,
+                 pw.mom[2], pw.mom[3], pb.rec, pb.rec_mask};
+    cudaMemsetAsync(pb.hot, 0, sizeof(uint32_t), st);
     dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY);
     k_papply<<<g, dim3(BX, BY), 0, st>>>(aa);
+    k_papply_hot<<<152 * 4, 32 * HOT_WARPS, 0, st>>>(aa);
     k_pfinal<<<pgrid, PB, 0, st>>>(es, pb.d, n, pb.rec, pb.rec_mask);
-    count_launch(8);
+    count_launch(9);
 }
 
 void launch_particle_smooth(const StepConsts& c, float count, const PWorld& in, const PWorld& out, cudaStream_t st) {

@@ -71,6 +71,19 @@ def test_particles_crowded_texels_and_kills():
     assert it.max() <= 6
 
 
+def test_particles_pile_up_beyond_shared_sort():
+    # 16384 droplets on an 8x8 map: every live droplet sits on the same few
+    # texels, buckets of thousands of records (above the 2048 a warp sorts in
+    # shared memory)
+    s = H.settings_particles()
+    s.Kspeed[0] = 0.0
+    w, ow, os_, oo = make(8, 16384, s, seed=5)
+    for k in range(3):
+        w.step(1, H.MODE_PARTICLES)
+        ow.particle_step(os_, oo, 1)
+        check(w, ow, f"pile-up step {k + 1}")
+
+
 def test_particles_rain_off_keeps_idle_and_limits():
     s = H.settings_particles()
     w, ow, os_, oo = make(64, 256, s, rain=False)
