@@ -95,7 +95,7 @@ struct ParticleBufs {
     uint32_t* block_sums;  // particle_scan_blocks(n*n)
     uint32_t* keys;        // 4*count records (droplet * 4 + corner), bucketed by texel
     uint32_t* sorted;      // 4*count: hot texels' buckets in droplet-id order
-    uint32_t* hot;         // 1 + hot_cap: count of hot texels, then their indices
+    uint32_t* hot;         // 2 + 2*hot_cap: counts of mid and big texels, then their indices
     uint32_t hot_cap;      // particle_hot_capacity(n*n, count)
     float* rec;            // 8*count: per record the dirt and rock sediment it left
     uint8_t* rec_mask;     // 4*count: which layers a record set

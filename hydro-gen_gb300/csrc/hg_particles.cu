@@ -8,13 +8,14 @@
 // no thread waits on another:
 //   k_pcount / scan / k_pscatter   counting sort of the droplets' four corner
 //                                  records by texel
-//   k_papply / k_papply_hot        each texel applies its records in
+//   k_papply / _mid / _big         each texel applies its records in
 //                                  droplet-id order (a texel update needs only
 //                                  the droplet's state from before the pass)
 //                                  and stores what each corner left for the
 //                                  droplet's sediment; a texel with up to 8
-//                                  records sorts them in registers, busier
-//                                  ones get a warp each
+//                                  records sorts them in its thread's
+//                                  registers, up to 32 across a warp's lanes,
+//                                  more in a warp's shared memory
 //   k_pfinal                       each droplet replays its corners 0..3
 // which is a sequential pass over droplets in id order, corners in order.
 // Spawn positions come from Philox4x32-10 (counter: droplet id, step,
@@ -255,8 +256,9 @@ struct ApplyArgs {
     int n;
     const uint32_t* offs;  // n*n + 1
     const uint32_t* keys;  // records bucketed by texel, any order within a bucket
-    uint32_t* sorted;      // hot texels: their bucket in droplet-id order
-    uint32_t* hot;         // [0]: hot texel count, then the hot texels
+    uint32_t* sorted;      // big texels: their bucket in droplet-id order
+    uint32_t* hot;         // [0], [1]: mid and big texel counts; then mid texels
+                           // from [2], big texels from [2 + hot_cap]
     uint32_t hot_cap;
     float* rock;
     float* dirt;
@@ -294,9 +296,15 @@ struct Texel {
     float terr[2], wat, mz, mw;
 };
 
+// what a record leaves for its droplet's sediment replay
+struct RecOut {
+    float s_dirt, s_rock;
+    uint32_t mask;
+};
+
 // one droplet corner on its texel (glsl/particle_erosion.glsl:66-122): the
 // layer loop from dirt down to rock, then water and momentum
-__device__ __forceinline__ void apply_record(const ApplyArgs& a, const Rec& r, Texel& T) {
+__device__ __forceinline__ RecOut apply_record(const ApplyArgs& a, const Rec& r, Texel& T) {
     const float old_sed[2] = {r.s0, r.s1};
     float s_out[2] = {0.0f, 0.0f};
     uint32_t mask = 0;
@@ -330,12 +338,16 @@ __device__ __forceinline__ void apply_record(const ApplyArgs& a, const Rec& r, T
         }
         s_out[l] = s1;
     }
-    a.rec[2 * r.key + 0] = s_out[1];
-    a.rec[2 * r.key + 1] = s_out[0];
-    a.rec_mask[r.key] = (uint8_t)mask;
     T.wat += 1e-5f * r.vol * r.multipl;
     T.mz += r.vol * r.vx * r.multipl;
     T.mw += r.vol * r.vy * r.multipl;
+    return RecOut{s_out[1], s_out[0], mask};
+}
+
+__device__ __forceinline__ void store_rec(const ApplyArgs& a, uint32_t key, const RecOut& o) {
+    a.rec[2 * key + 0] = o.s_dirt;
+    a.rec[2 * key + 1] = o.s_rock;
+    a.rec_mask[key] = (uint8_t)o.mask;
 }
 
 __device__ __forceinline__ Texel load_texel(const ApplyArgs& a, size_t t) {
@@ -350,9 +362,10 @@ __device__ __forceinline__ void store_texel(const ApplyArgs& a, size_t t, const 
 }
 
 constexpr int SMALL = 8;  // records a texel's own thread sorts and applies
+constexpr int MID = 32;   // records a warp sorts in registers
 
 // each texel with at most SMALL records applies them in droplet-id order;
-// busier texels go to the hot list
+// busier texels go to the mid (up to MID records) or big lists
 __global__ void k_papply(const ApplyArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = a.n;
@@ -362,8 +375,9 @@ __global__ void k_papply(const ApplyArgs a) {
     if (lo == hi) return;
     const uint32_t k = hi - lo;
     if (k > SMALL) {
-        const uint32_t slot = atomicAdd(a.hot, 1u);
-        if (slot < a.hot_cap) a.hot[1 + slot] = (uint32_t)t;
+        const int big = k > (uint32_t)MID ? 1 : 0;
+        const uint32_t slot = atomicAdd(a.hot + big, 1u);
+        if (slot < a.hot_cap) a.hot[2 + big * a.hot_cap + slot] = (uint32_t)t;
         return;
     }
     uint32_t kk[SMALL];
@@ -381,24 +395,65 @@ __global__ void k_papply(const ApplyArgs a) {
     Texel T = load_texel(a, t);
 #pragma unroll
     for (int i = 0; i < SMALL; ++i)
-        if ((uint32_t)i < k) apply_record(a, load_rec(a, kk[i]), T);
+        if ((uint32_t)i < k) store_rec(a, kk[i], apply_record(a, load_rec(a, kk[i]), T));
     store_texel(a, t, T);
 }
 
-constexpr int HOT_WARPS = 4;     // warps per block of k_papply_hot
+constexpr int HOT_WARPS = 4;     // warps per block of the mid / big kernels
 constexpr int HOT_KEYS = 2048;   // bucket size a warp sorts in shared memory
 
-// one warp per hot texel: sort the bucket by droplet id (bitonic network in
-// shared memory; buckets above HOT_KEYS by rank counting over global
-// memory), then stage 32 records at a time in shared memory for lane 0's
-// sequential update
-__global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_hot(const ApplyArgs a) {
+// one warp per mid texel (SMALL < records <= 32): lane i holds record i;
+// a bitonic network over the lanes sorts the keys by droplet id, each lane
+// loads its record, and the warp runs the texel's sequential update in
+// lockstep with record i broadcast from lane i
+__global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_mid(const ApplyArgs a) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint32_t nmid = min(a.hot[0], a.hot_cap);
+    for (uint32_t h = blockIdx.x * HOT_WARPS + wl; h < nmid; h += gridDim.x * HOT_WARPS) {
+        const size_t t = a.hot[2 + h];
+        const uint32_t lo = a.offs[t], k = a.offs[t + 1] - lo;
+        uint32_t key = (uint32_t)lane < k ? a.keys[lo + lane] : 0xffffffffu;
+#pragma unroll
+        for (int size = 2; size <= 32; size <<= 1)
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                const uint32_t other = __shfl_xor_sync(FULL, key, stride);
+                const bool up = (lane & size) == 0, lower = (lane & stride) == 0;
+                key = (lower == up) ? min(key, other) : max(key, other);
+            }
+        Rec mine{};
+        if ((uint32_t)lane < k) mine = load_rec(a, key);
+        Texel T = load_texel(a, t);
+        for (uint32_t i = 0; i < k; ++i) {
+            Rec r;
+            r.key = __shfl_sync(FULL, mine.key, i);
+            r.multipl = __shfl_sync(FULL, mine.multipl, i);
+            r.sc = __shfl_sync(FULL, mine.sc, i);
+            r.vol = __shfl_sync(FULL, mine.vol, i);
+            r.s0 = __shfl_sync(FULL, mine.s0, i);
+            r.s1 = __shfl_sync(FULL, mine.s1, i);
+            r.vx = __shfl_sync(FULL, mine.vx, i);
+            r.vy = __shfl_sync(FULL, mine.vy, i);
+            r.kill = __shfl_sync(FULL, mine.kill, i);
+            const RecOut o = apply_record(a, r, T);
+            if ((uint32_t)lane == i) store_rec(a, r.key, o);
+        }
+        if (lane == 0) store_texel(a, t, T);
+    }
+}
+
+// one warp per big texel (more than 32 records): sort the bucket by droplet
+// id (bitonic network in shared memory; buckets above HOT_KEYS by rank
+// counting over global memory), then stage 32 records at a time in shared
+// memory for lane 0's sequential update
+__global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_big(const ApplyArgs a) {
     __shared__ uint32_t sk[HOT_WARPS][HOT_KEYS];
     __shared__ Rec sr[HOT_WARPS][32];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const uint32_t nhot = min(a.hot[0], a.hot_cap);
-    for (uint32_t h = blockIdx.x * HOT_WARPS + wl; h < nhot; h += gridDim.x * HOT_WARPS) {
-        const size_t t = a.hot[1 + h];
+    const uint32_t nbig = min(a.hot[1], a.hot_cap);
+    for (uint32_t h = blockIdx.x * HOT_WARPS + wl; h < nbig; h += gridDim.x * HOT_WARPS) {
+        const size_t t = a.hot[2 + a.hot_cap + h];
         const uint32_t lo = a.offs[t], hi = a.offs[t + 1], k = hi - lo;
         if (k <= (uint32_t)HOT_KEYS) {
             uint32_t P = 32;
@@ -434,7 +489,7 @@ __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_hot(const ApplyArgs a
             if ((uint32_t)lane < m) sr[wl][lane] = load_rec(a, a.sorted[base + lane]);
             __syncwarp();
             if (lane == 0)
-                for (uint32_t i = 0; i < m; ++i) apply_record(a, sr[wl][i], T);
+                for (uint32_t i = 0; i < m; ++i) store_rec(a, sr[wl][i].key, apply_record(a, sr[wl][i], T));
             __syncwarp();
         }
         if (lane == 0) store_texel(a, t, T);
@@ -541,12 +596,13 @@ void launch_particle_step(const StepConsts& c, const hg_erosion_settings& es, co
     k_pscatter<<<pgrid, PB, 0, st>>>(pb.d, n, pb.cursor, pb.keys);
     ApplyArgs aa{es, pb.d, n, pb.offs, pb.keys, pb.sorted, pb.hot, pb.hot_cap, pw.rock, pw.dirt, pw.water,
                  pw.mom[2], pw.mom[3], pb.rec, pb.rec_mask};
-    cudaMemsetAsync(pb.hot, 0, sizeof(uint32_t), st);
+    cudaMemsetAsync(pb.hot, 0, 2 * sizeof(uint32_t), st);
     dim3 g((n + BX - 1) / BX, (n + BY - 1) / BY);
     k_papply<<<g, dim3(BX, BY), 0, st>>>(aa);
-    k_papply_hot<<<152 * 4, 32 * HOT_WARPS, 0, st>>>(aa);
+    k_papply_mid<<<152 * 12, 32 * HOT_WARPS, 0, st>>>(aa);
+    k_papply_big<<<152 * 4, 32 * HOT_WARPS, 0, st>>>(aa);
     k_pfinal<<<pgrid, PB, 0, st>>>(es, pb.d, n, pb.rec, pb.rec_mask);
-    count_launch(9);
+    count_launch(10);
 }
 
 void launch_particle_smooth(const StepConsts& c, float count, const PWorld& in, const PWorld& out, cudaStream_t st) {

@@ -1027,7 +1027,7 @@ int hg_particles_init(hg_world* w, int count) {
     P->b.keys = (uint32_t*)take(4 * cnt * sizeof(uint32_t));
     P->b.sorted = (uint32_t*)take(4 * cnt * sizeof(uint32_t));
     P->b.hot_cap = (uint32_t)particle_hot_capacity(cl, count);
-    P->b.hot = (uint32_t*)take((1 + (size_t)P->b.hot_cap) * sizeof(uint32_t));
+    P->b.hot = (uint32_t*)take((2 + 2 * (size_t)P->b.hot_cap) * sizeof(uint32_t));
     P->b.rec = (float*)take(8 * cnt * sizeof(float));
     P->b.rec_mask = (uint8_t*)take(4 * cnt);
     for (int k = 0; k < 2; ++k)
