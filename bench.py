@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--n", type=int, default=N_GRID)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
+    ap.add_argument("--extra", choices=["particles", "render"], default=None,
+                    help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
+                         "and print its JSON; for profiling captures")
     return ap.parse_args()
 
 
@@ -364,6 +367,8 @@ def bench_particles(H, torch, n=1024, count=262144, nsteps=200, warmup=10, cpu_b
                        "thermal both layers + smoothing", "steps": nsteps,
            "droplet_steps_per_s": count * nsteps / el, "ms_per_step": 1e3 * el / nsteps,
            "launches_per_step": launches / nsteps}
+    if cpu_budget_s <= 0:
+        return out
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     ow = O.OracleWorld(n, 32)
@@ -385,7 +390,7 @@ def bench_particles(H, torch, n=1024, count=262144, nsteps=200, warmup=10, cpu_b
     return out
 
 
-def bench_render(H, torch, n=1024, width=1920, height=1080, frames=20, cpu_budget_s=6.0):
+def bench_render(H, torch, n=1024, width=1920, height=1080, frames=20, warmup=3, cpu_budget_s=6.0):
     """The headless ray-marcher on a 1024^2 two-layer world from the
     reference's terrain generator with a lake (water filled to height 96, the
     reference's WATER_HEIGHT), 1920x1080 from inside the map over the lake; the
@@ -403,7 +408,7 @@ def bench_render(H, torch, n=1024, width=1920, height=1080, frames=20, cpu_budge
     def frame():
         H.check(H.lib.hg_render_device(w.h, H.ctypes.byref(cam), width, height, img.data_ptr(), None))
 
-    for _ in range(3):
+    for _ in range(warmup):
         frame()
     w.sync()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -426,6 +431,8 @@ def bench_render(H, torch, n=1024, width=1920, height=1080, frames=20, cpu_budge
            "e2e": {"ms_per_frame": e2e_ms, "mpixels_per_s": mpix / (e2e_ms / 1e3),
                    "d2h_bytes_per_frame": width * height * 4},
            }
+    if cpu_budget_s <= 0:
+        return out
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     cw, ch = width // 10, height // 10
@@ -478,6 +485,15 @@ def main():
     import hydrogen as H
 
     torch.cuda.set_device(local)
+    if args.extra is not None:
+        if rank == 0:
+            budget = 0.0 if args.no_cpu_baseline else 6.0
+            if args.extra == "particles":
+                out = bench_particles(H, torch, nsteps=args.steps, warmup=args.warmup, cpu_budget_s=budget)
+            else:
+                out = bench_render(H, torch, frames=args.steps, warmup=args.warmup, cpu_budget_s=budget)
+            print(json.dumps(out), flush=True)
+        return
     dist = None
     if world_size > 1:
         import torch.distributed as dist
