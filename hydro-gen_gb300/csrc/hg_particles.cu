@@ -344,6 +344,89 @@ __device__ __forceinline__ RecOut apply_record(const ApplyArgs& a, const Rec& r,
     return RecOut{s_out[1], s_out[0], mask};
 }
 
+// A record's update with its texel-independent parts computed ahead (in
+// parallel across a warp's lanes): the dirt step with no layer exhausted,
+// then the rock step.  mode 0: kill (both layers take their share back);
+// 1: dirt dissolves and the loop breaks; 2: dirt deposits, rock dissolves;
+// 3: both deposit.  Only an exhausted dirt layer (mode 1 going below zero)
+// needs the full update, apply_record.
+struct Pre {
+    uint32_t key;
+    int mode;
+    float d1, d0;    // kill: the returned sediment; else the dissolved / deposited amounts
+    float s1n, s0n;  // the dirt / rock sediment after their step
+    float wi, mzi, mwi;
+};
+
+__device__ __forceinline__ Pre prep_record(const ApplyArgs& a, const Rec& r) {
+    Pre p;
+    p.key = r.key;
+    p.wi = 1e-5f * r.vol * r.multipl;
+    p.mzi = r.vol * r.vx * r.multipl;
+    p.mwi = r.vol * r.vy * r.multipl;
+    p.s1n = 0.0f;
+    p.s0n = 0.0f;
+    if (r.kill) {
+        p.mode = 0;
+        p.d1 = r.s1 * r.multipl;
+        p.d0 = r.s0 * r.multipl;
+        return p;
+    }
+    const float c = gmax(0.0f, r.sc - 0.0f);  // cap is 0 until a layer is exhausted
+    if (c > r.s1) {
+        p.mode = 1;
+        p.d1 = r.multipl * (a.es.d_t * a.es.Ks[1]) * (c - r.s1);
+        p.s1n = r.s1 + p.d1;
+        p.d0 = 0.0f;
+        return p;
+    }
+    p.d1 = r.multipl * (a.es.d_t * a.es.Kd[1]) * (r.s1 - c);
+    p.s1n = r.s1 - p.d1;
+    if (c > r.s0) {
+        p.mode = 2;
+        p.d0 = r.multipl * (a.es.d_t * a.es.Ks[0]) * (c - r.s0);
+        p.s0n = r.s0 + p.d0;
+    } else {
+        p.mode = 3;
+        p.d0 = r.multipl * (a.es.d_t * a.es.Kd[0]) * (r.s0 - c);
+        p.s0n = r.s0 - p.d0;
+    }
+    return p;
+}
+
+// the texel-dependent rest of a prepared record; false (texel untouched)
+// when the dirt layer would be exhausted
+__device__ __forceinline__ bool apply_prepared(const Pre& p, Texel& T, RecOut& o) {
+    if (p.mode == 1) {
+        const float t = T.terr[1] - p.d1;
+        if (t < 0.0f) return false;
+        T.terr[1] = t;
+        o = RecOut{p.s1n, 0.0f, 2u};
+    } else if (p.mode == 0) {
+        T.terr[1] += p.d1;
+        T.terr[0] += p.d0;
+        o = RecOut{0.0f, 0.0f, 0u};
+    } else if (p.mode == 2) {
+        T.terr[1] += p.d1;
+        const float t = T.terr[0] - p.d0;
+        if (t < 0.0f) {
+            o = RecOut{p.s1n, p.s0n + t, 3u};
+            T.terr[0] = 0.0f;
+        } else {
+            o = RecOut{p.s1n, p.s0n, 3u};
+            T.terr[0] = t;
+        }
+    } else {
+        T.terr[1] += p.d1;
+        T.terr[0] += p.d0;
+        o = RecOut{p.s1n, p.s0n, 3u};
+    }
+    T.wat += p.wi;
+    T.mz += p.mzi;
+    T.mw += p.mwi;
+    return true;
+}
+
 __device__ __forceinline__ void store_rec(const ApplyArgs& a, uint32_t key, const RecOut& o) {
     a.rec[2 * key + 0] = o.s_dirt;
     a.rec[2 * key + 1] = o.s_rock;
@@ -405,7 +488,7 @@ constexpr int HOT_KEYS = 2048;   // bucket size a warp sorts in shared memory
 // one warp per mid texel (SMALL < records <= 32): lane i holds record i;
 // a bitonic network over the lanes sorts the keys by droplet id, each lane
 // loads its record, and the warp runs the texel's sequential update in
-// lockstep with record i broadcast from lane i
+// lockstep with record i's prepared update broadcast from lane i
 __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_mid(const ApplyArgs a) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
@@ -424,20 +507,34 @@ __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_mid(const ApplyArgs a
             }
         Rec mine{};
         if ((uint32_t)lane < k) mine = load_rec(a, key);
+        const Pre mp = prep_record(a, mine);
         Texel T = load_texel(a, t);
         for (uint32_t i = 0; i < k; ++i) {
-            Rec r;
-            r.key = __shfl_sync(FULL, mine.key, i);
-            r.multipl = __shfl_sync(FULL, mine.multipl, i);
-            r.sc = __shfl_sync(FULL, mine.sc, i);
-            r.vol = __shfl_sync(FULL, mine.vol, i);
-            r.s0 = __shfl_sync(FULL, mine.s0, i);
-            r.s1 = __shfl_sync(FULL, mine.s1, i);
-            r.vx = __shfl_sync(FULL, mine.vx, i);
-            r.vy = __shfl_sync(FULL, mine.vy, i);
-            r.kill = __shfl_sync(FULL, mine.kill, i);
-            const RecOut o = apply_record(a, r, T);
-            if ((uint32_t)lane == i) store_rec(a, r.key, o);
+            Pre q;
+            q.key = __shfl_sync(FULL, mp.key, i);
+            q.mode = __shfl_sync(FULL, mp.mode, i);
+            q.d1 = __shfl_sync(FULL, mp.d1, i);
+            q.d0 = __shfl_sync(FULL, mp.d0, i);
+            q.s1n = __shfl_sync(FULL, mp.s1n, i);
+            q.s0n = __shfl_sync(FULL, mp.s0n, i);
+            q.wi = __shfl_sync(FULL, mp.wi, i);
+            q.mzi = __shfl_sync(FULL, mp.mzi, i);
+            q.mwi = __shfl_sync(FULL, mp.mwi, i);
+            RecOut o;
+            if (!apply_prepared(q, T, o)) {  // uniform: every lane holds the same texel state
+                Rec r;
+                r.key = q.key;
+                r.multipl = __shfl_sync(FULL, mine.multipl, i);
+                r.sc = __shfl_sync(FULL, mine.sc, i);
+                r.vol = __shfl_sync(FULL, mine.vol, i);
+                r.s0 = __shfl_sync(FULL, mine.s0, i);
+                r.s1 = __shfl_sync(FULL, mine.s1, i);
+                r.vx = __shfl_sync(FULL, mine.vx, i);
+                r.vy = __shfl_sync(FULL, mine.vy, i);
+                r.kill = __shfl_sync(FULL, mine.kill, i);
+                o = apply_record(a, r, T);
+            }
+            if ((uint32_t)lane == i) store_rec(a, q.key, o);
         }
         if (lane == 0) store_texel(a, t, T);
     }
@@ -450,6 +547,7 @@ __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_mid(const ApplyArgs a
 __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_big(const ApplyArgs a) {
     __shared__ uint32_t sk[HOT_WARPS][HOT_KEYS];
     __shared__ Rec sr[HOT_WARPS][32];
+    __shared__ Pre sp[HOT_WARPS][32];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const uint32_t nbig = min(a.hot[1], a.hot_cap);
     for (uint32_t h = blockIdx.x * HOT_WARPS + wl; h < nbig; h += gridDim.x * HOT_WARPS) {
@@ -486,10 +584,18 @@ __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_big(const ApplyArgs a
         Texel T = load_texel(a, t);
         for (uint32_t base = lo; base < hi; base += 32) {
             const uint32_t m = min(32u, hi - base);
-            if ((uint32_t)lane < m) sr[wl][lane] = load_rec(a, a.sorted[base + lane]);
+            if ((uint32_t)lane < m) {
+                const Rec r = load_rec(a, a.sorted[base + lane]);
+                sr[wl][lane] = r;
+                sp[wl][lane] = prep_record(a, r);
+            }
             __syncwarp();
             if (lane == 0)
-                for (uint32_t i = 0; i < m; ++i) store_rec(a, sr[wl][i].key, apply_record(a, sr[wl][i], T));
+                for (uint32_t i = 0; i < m; ++i) {
+                    RecOut o;
+                    if (!apply_prepared(sp[wl][i], T, o)) o = apply_record(a, sr[wl][i], T);
+                    store_rec(a, sp[wl][i].key, o);
+                }
             __syncwarp();
         }
         if (lane == 0) store_texel(a, t, T);
