@@ -134,16 +134,57 @@ __device__ __forceinline__ float4 tex_bilinear(const Scene& S, float px, float p
     if (!(px > -2.0f && px < (float)S.n + 1.0f && py > -2.0f && py < (float)S.n + 1.0f)) return z;
     const int ix = (int)px, iy = (int)py;
     const float fx = fract_(px), fy = fract_(py);
-    auto t = [&](int x, int y) {
-        return (x >= 0 && x < S.n && y >= 0 && y < S.n) ? __ldg(S.hm + (size_t)y * S.n + x) : z;
-    };
-    const float4 a = t(ix, iy), b = t(ix + 1, iy), c = t(ix, iy + 1), d = t(ix + 1, iy + 1);
+    float4 a, b, c, d;
+    if ((unsigned)ix < (unsigned)(S.n - 1) && (unsigned)iy < (unsigned)(S.n - 1)) {  // all four taps inside
+        const float4* q = S.hm + (size_t)iy * S.n + ix;
+        a = __ldg(q);
+        b = __ldg(q + 1);
+        c = __ldg(q + S.n);
+        d = __ldg(q + S.n + 1);
+    } else {
+        auto t = [&](int x, int y) {
+            return (x >= 0 && x < S.n && y >= 0 && y < S.n) ? __ldg(S.hm + (size_t)y * S.n + x) : z;
+        };
+        a = t(ix, iy);
+        b = t(ix + 1, iy);
+        c = t(ix, iy + 1);
+        d = t(ix + 1, iy + 1);
+    }
     float4 r;
     r.x = gmix(gmix(a.x, b.x, fx), gmix(c.x, d.x, fx), fy);
     r.y = gmix(gmix(a.y, b.y, fx), gmix(c.y, d.y, fx), fy);
     r.z = gmix(gmix(a.z, b.z, fx), gmix(c.z, d.z, fx), fy);
     r.w = gmix(gmix(a.w, b.w, fx), gmix(c.w, d.w, fx), fy);
     return r;
+}
+
+// the march's height at (px, py): rock + dirt (terrain rays) or the total
+// (primary rays), the same bilinear channels tex_bilinear gives
+__device__ __forceinline__ float tex_height(const Scene& S, float px, float py, bool terrain) {
+    if (!(px > -2.0f && px < (float)S.n + 1.0f && py > -2.0f && py < (float)S.n + 1.0f))
+        return terrain ? 0.0f + 0.0f : 0.0f;
+    const int ix = (int)px, iy = (int)py;
+    const float fx = fract_(px), fy = fract_(py);
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 a, b, c, d;
+    if ((unsigned)ix < (unsigned)(S.n - 1) && (unsigned)iy < (unsigned)(S.n - 1)) {
+        const float4* q = S.hm + (size_t)iy * S.n + ix;
+        a = __ldg(q);
+        b = __ldg(q + 1);
+        c = __ldg(q + S.n);
+        d = __ldg(q + S.n + 1);
+    } else {
+        auto t = [&](int x, int y) {
+            return (x >= 0 && x < S.n && y >= 0 && y < S.n) ? __ldg(S.hm + (size_t)y * S.n + x) : z;
+        };
+        a = t(ix, iy);
+        b = t(ix + 1, iy);
+        c = t(ix, iy + 1);
+        d = t(ix + 1, iy + 1);
+    }
+    if (terrain)
+        return gmix(gmix(a.x, b.x, fx), gmix(c.x, d.x, fx), fy) + gmix(gmix(a.y, b.y, fx), gmix(c.y, d.y, fx), fy);
+    return gmix(gmix(a.w, b.w, fx), gmix(c.w, d.w, fx), fy);
 }
 
 __device__ __forceinline__ float2 sed_bilinear(const Scene& S, float px, float py) {
@@ -169,29 +210,35 @@ struct Ray {
 // raymarch (glsl/rendering.glsl:462-516)
 __device__ __noinline__ Ray raymarch(const Scene S, V3 o, V3 d, float max_d, int max_iter, int kind) {
     float dist = 0.001f, d_dist = 0.1f;
-    if (kind == KIND_TERRAIN) {
+    const bool terrain = kind == KIND_TERRAIN;
+    if (terrain) {
         dist = 0.0f;
         d_dist = 0.1e-12f;
     }
     float min_sdf = 1.0f;
-    float4 terr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // each step needs only the marched height; the full texel (terr) is
+    // sampled again where the ray stops
+    V3 last = o;
+    bool sampled = false;
     for (int i = 0; i < max_iter; ++i) {
         const V3 sp = add(o, scl(d, dist));
-        terr = tex_bilinear(S, sp.x, sp.z);
-        const float t_height = kind == KIND_TERRAIN ? terr.x + terr.y : terr.w;
+        const float t_height = tex_height(S, sp.x, sp.z, terrain);
+        last = sp;
+        sampled = true;
         if ((sp.y > S.max_height && d.y >= 0.0f) || (sp.y <= 0.0f && d.y < 0.0f)) break;
         const float d_height = sp.y - t_height;
         if (fabsf(d_height) <= 0.05f) {
             const V3 q = sub(sp, scl(d, 0.05f));
             return Ray{q, 0.0f, dist - 0.05f, tex_bilinear(S, q.x, q.z)};
         } else if (d_height < 0.0f) {
-            return Ray{add(o, scl(d, dist)), min_sdf, dist, terr};
+            return Ray{add(o, scl(d, dist)), min_sdf, dist, tex_bilinear(S, sp.x, sp.z)};
         }
         min_sdf = gmin(min_sdf, 12.0f * d_dist / dist);
-        if (dist > max_d) return Ray{sp, min_sdf, max_d, terr};
+        if (dist > max_d) return Ray{sp, min_sdf, max_d, tex_bilinear(S, sp.x, sp.z)};
         d_dist = S.prec * d_height;
         dist += d_dist;
     }
+    const float4 terr = sampled ? tex_bilinear(S, last.x, last.z) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     return Ray{add(o, scl(d, max_d)), min_sdf, max_d, terr};
 }
 
