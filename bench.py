@@ -580,7 +580,7 @@ def main():
         "plain_ms_per_step": plain_ms / plain_steps,
         "pct_hbm_peak": 100.0 * achieved / peak,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "kernel": "fused step = k_hydro + k_transport launch pair (39 % / 61 % of its time, ncu "
+                     "kernel": "fused step = k_hydro + k_transport launch pair (49 % / 51 % of its time, ncu "
                                "launch list); achieved = 72 B x cells / ms per step",
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "traffic": tpc * cells if tpc else None,
