@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=N_GRID)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
-    ap.add_argument("--extra", choices=["particles", "render"], default=None,
+    ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain"], default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
     return ap.parse_args()
@@ -339,6 +339,99 @@ def bench_batch(H, torch, count=64, nsteps=50, warmup=16):
     return out
 
 
+def bench_two_layer(H, torch, n=4096, nsteps=100, warmup=10, cpu_budget_s=6.0, cpu_n=1024):
+    """The reference's own model: a two-layer (rock + dirt) world from its
+    terrain generator with its default grid settings (src/state.cpp:81-92:
+    Kconv 0.001, slippage 0.5 / 2.0, so both talus layers and smoothing run)
+    and uniform rain of 0.01 every step, per-pass kernels; the float oracle
+    steps a 1024^2 world of the same model on the host."""
+    w = H.World(n, layers=2)
+    w.init_reference_heightmap(H.map_settings(hmap_dims=(n, n)))
+    s = H.ErosionSettings()
+    H.check(H.lib.hg_default_erosion_settings(H.ctypes.byref(s)))
+    w.set_erosion(s)
+    w.set_rain(H.rain_uniform(0.01, 1))
+    w.set_options(H.options(H.RAIN_UNIFORM))
+    w.step(warmup, H.MODE_PLAIN)
+    w.sync()
+    stream = torch.cuda.ExternalStream(w.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = H.lib.hg_launch_count()
+    e0.record(stream)
+    w.step(nsteps, H.MODE_PLAIN)
+    e1.record(stream)
+    e1.synchronize()
+    launches = H.lib.hg_launch_count() - l0
+    ms = e0.elapsed_time(e1) / nsteps
+    w.close()
+    cells = n * n
+    peak, kind = peaks()
+    achieved = 88.0 * cells / (ms / 1e3) / 1e9  # 11 fields x 4 B x (read + write)
+    out = {"workload": f"{n}x{n} two-layer world (reference terrain), reference grid defaults, uniform rain 0.01",
+           "steps": nsteps, "ms_per_step": ms, "cell_steps_per_s": cells / (ms / 1e3),
+           "launches_per_step": launches / nsteps,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "algorithmic_bytes_per_cell_step": 88, "peak_source": f"{kind} hbm_gbs"}}
+    if cpu_budget_s <= 0:
+        return out
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    rock, dirt = O.ref_heightmap(H.map_settings(hmap_dims=(cpu_n, cpu_n)), cpu_n)
+    ow = O.OracleWorld(cpu_n, 32)
+    ow.set("rock", rock)
+    ow.set("dirt", dirt)
+    os_, oo = O.erosion_from(s), O.options(1, 1, 0.01)
+    ow.step(os_, oo, 1)
+    k, t0 = 0, time.perf_counter()
+    while True:
+        ow.step(os_, oo, 1)
+        k += 1
+        if time.perf_counter() - t0 >= cpu_budget_s and k >= 2:
+            break
+    cel = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": k * cpu_n * cpu_n / cel, "unit": "cell-steps/s", "cores": O.num_threads(),
+                           "kind": "port", "sample": f"{cpu_n}x{cpu_n} world of the same model, {k} steps in "
+                           f"{cel:.1f} s (float oracle, OpenMP over rows)"}
+    return out
+
+
+def bench_terrain(H, torch, n=4096, reps=5, cpu_budget_s=4.0, cpu_n=512):
+    """The reference's terrain generator (glsl/heightmap.glsl, default map
+    settings: 8 octaves of derivative-damped gradient noise with domain warp)
+    on a 4096^2 two-layer world; the oracle generates a 512^2 map."""
+    w = H.World(n, layers=2)
+    ms_ = H.map_settings(hmap_dims=(n, n))
+    w.init_reference_heightmap(ms_)
+    w.sync()
+    stream = torch.cuda.ExternalStream(w.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        w.init_reference_heightmap(ms_)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    w.close()
+    out = {"workload": f"reference terrain generator, {n}x{n}, default map settings", "ms": ms,
+           "cells_per_s": n * n / (ms / 1e3)}
+    if cpu_budget_s <= 0:
+        return out
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    m2 = H.map_settings(hmap_dims=(cpu_n, cpu_n))
+    k, t0 = 0, time.perf_counter()
+    while True:
+        O.ref_heightmap(m2, cpu_n)
+        k += 1
+        if time.perf_counter() - t0 >= cpu_budget_s:
+            break
+    cel = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": k * cpu_n * cpu_n / cel, "unit": "cells/s", "cores": O.num_threads(),
+                           "kind": "port", "sample": f"{cpu_n}x{cpu_n} map, {k} maps in {cel:.1f} s (float oracle, "
+                           "OpenMP over rows)"}
+    return out
+
+
 def bench_particles(H, torch, n=1024, count=262144, nsteps=200, warmup=10, cpu_budget_s=6.0):
     """Droplet erosion (the reference's "particle" erosion type and default
     particle_count 262144) on a 1024^2 two-layer world from the reference's
@@ -490,6 +583,10 @@ def main():
             budget = 0.0 if args.no_cpu_baseline else 6.0
             if args.extra == "particles":
                 out = bench_particles(H, torch, nsteps=args.steps, warmup=args.warmup, cpu_budget_s=budget)
+            elif args.extra == "two_layer":
+                out = bench_two_layer(H, torch, nsteps=args.steps, warmup=args.warmup, cpu_budget_s=budget)
+            elif args.extra == "terrain":
+                out = bench_terrain(H, torch, reps=args.steps, cpu_budget_s=budget)
             else:
                 out = bench_render(H, torch, frames=args.steps, warmup=args.warmup, cpu_budget_s=budget)
             print(json.dumps(out), flush=True)
@@ -594,6 +691,8 @@ def main():
         line["fwd_adjoint"] = bench_adjoint(H, torch)
         line["batch"] = bench_batch(H, torch)
         line["large"] = bench_large(H, torch)
+        line["two_layer"] = bench_two_layer(H, torch)
+        line["terrain"] = bench_terrain(H, torch)
         line["particles"] = bench_particles(H, torch)
         line["render"] = bench_render(H, torch)
     if not args.no_cpu_baseline:
