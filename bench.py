@@ -343,35 +343,39 @@ def bench_two_layer(H, torch, n=4096, nsteps=100, warmup=10, cpu_budget_s=6.0, c
     """The reference's own model: a two-layer (rock + dirt) world from its
     terrain generator with its default grid settings (src/state.cpp:81-92:
     Kconv 0.001, slippage 0.5 / 2.0, so both talus layers and smoothing run)
-    and uniform rain of 0.01 every step, per-pass kernels; the float oracle
-    steps a 1024^2 world of the same model on the host."""
-    w = H.World(n, layers=2)
-    w.init_reference_heightmap(H.map_settings(hmap_dims=(n, n)))
+    and uniform rain of 0.01 every step; the fused three-kernel step and the
+    per-pass kernels.  The float oracle steps a 1024^2 world of the same
+    model on the host."""
     s = H.ErosionSettings()
     H.check(H.lib.hg_default_erosion_settings(H.ctypes.byref(s)))
-    w.set_erosion(s)
-    w.set_rain(H.rain_uniform(0.01, 1))
-    w.set_options(H.options(H.RAIN_UNIFORM))
-    w.step(warmup, H.MODE_PLAIN)
-    w.sync()
-    stream = torch.cuda.ExternalStream(w.stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = H.lib.hg_launch_count()
-    e0.record(stream)
-    w.step(nsteps, H.MODE_PLAIN)
-    e1.record(stream)
-    e1.synchronize()
-    launches = H.lib.hg_launch_count() - l0
-    ms = e0.elapsed_time(e1) / nsteps
-    w.close()
     cells = n * n
     peak, kind = peaks()
-    achieved = 88.0 * cells / (ms / 1e3) / 1e9  # 11 fields x 4 B x (read + write)
     out = {"workload": f"{n}x{n} two-layer world (reference terrain), reference grid defaults, uniform rain 0.01",
-           "steps": nsteps, "ms_per_step": ms, "cell_steps_per_s": cells / (ms / 1e3),
-           "launches_per_step": launches / nsteps,
-           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                        "algorithmic_bytes_per_cell_step": 88, "peak_source": f"{kind} hbm_gbs"}}
+           "steps": nsteps}
+    for name, mode in (("plain", H.MODE_PLAIN), ("fused", H.MODE_FUSED)):
+        w = H.World(n, layers=2)
+        w.init_reference_heightmap(H.map_settings(hmap_dims=(n, n)))
+        w.set_erosion(s)
+        w.set_rain(H.rain_uniform(0.01, 1))
+        w.set_options(H.options(H.RAIN_UNIFORM))
+        w.step(warmup, mode)
+        w.sync()
+        stream = torch.cuda.ExternalStream(w.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = H.lib.hg_launch_count()
+        e0.record(stream)
+        w.step(nsteps, mode)
+        e1.record(stream)
+        e1.synchronize()
+        launches = H.lib.hg_launch_count() - l0
+        ms = e0.elapsed_time(e1) / nsteps
+        w.close()
+        achieved = 88.0 * cells / (ms / 1e3) / 1e9  # 11 fields x 4 B x (read + write)
+        out[name] = {"ms_per_step": ms, "cell_steps_per_s": cells / (ms / 1e3), "launches_per_step": launches / nsteps,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved / peak, "algorithmic_bytes_per_cell_step": 88,
+                                  "peak_source": f"{kind} hbm_gbs"}}
+    out["fused_vs_plain"] = out["plain"]["ms_per_step"] / out["fused"]["ms_per_step"]
     if cpu_budget_s <= 0:
         return out
     sys.path.insert(0, os.path.join(ROOT, "oracle"))

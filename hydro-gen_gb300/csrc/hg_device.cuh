@@ -136,6 +136,13 @@ struct StepConsts {
     float Kalpha1, Kspeed1;
 };
 
+// Layer 1's talus thresholds (as talus_x_cross, talus_b_diag, fast_div of
+// layer 0; kept out of StepConsts, which batch launches carry per terrain).
+struct Talus1 {
+    float x_cross, b_diag;
+    int fast_div;
+};
+
 // ---- hydro_flux, glsl/hydro_flux.glsl:77-166 -------------------------------------
 // w* are neighbour totals (rock + water after rain; FAR_HEIGHT outside the
 // grid), in* the neighbours' old flux facing this cell (left.fR, right.fL,
@@ -364,22 +371,21 @@ __device__ __forceinline__ ThermalOut cell_thermal_ref(const StepConsts& c, floa
 // quotients S*dh/bk share their divisor: with the operands in div_recip's
 // range they come from one reciprocal, else from IEEE division; either way
 // they are the correctly rounded quotients of the shader's expression.
-__device__ __forceinline__ void cell_thermal_outflows(const StepConsts& c, float b, const float nb[8], float o[8]) {
-    float dh[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];
+__device__ __forceinline__ void cell_thermal_outflows_dh(float dt, float Kalpha, float Kspeed, float x_cross,
+                                                        float b_diag, int fast_div, float terr, const float dh[8],
+                                                        float o[8]) {
     // H only matters when a direction is marked, i.e. some drop is >= a
     // positive threshold: then the shader's "if (dh > H) H = dh" from 0 and
     // fmaxf agree (NaN drops are skipped by both)
     float H = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; ++k) H = fmaxf(H, dh[k]);
-    H = gmin(b, H);
+    H = gmin(terr, H);
     // marked drops (0 where unmarked): sums and maxima over the marked set
     float dm[8], bk = 0.0f, max_cross = 0.0f, max_diag = 0.0f;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        dm[k] = dh[k] >= (k < 4 ? c.talus_x_cross : c.talus_b_diag) ? dh[k] : 0.0f;
+        dm[k] = dh[k] >= (k < 4 ? x_cross : b_diag) ? dh[k] : 0.0f;
         bk += dm[k];  // + 0 leaves the sum's bits unchanged (it starts at +0)
         if (k < 4) max_cross = fmaxf(max_cross, dm[k]);
         else max_diag = fmaxf(max_diag, dm[k]);
@@ -387,14 +393,14 @@ __device__ __forceinline__ void cell_thermal_outflows(const StepConsts& c, float
 #pragma unroll
     for (int k = 0; k < 8; ++k) o[k] = 0.0f;
     if (!(bk > 0.0f)) return;  // no marked direction (marked drops are > 0)
-    bool fast = c.fast_div && bk <= 0x1p40f;  // then max_diag is 0 or in [2^-30, 2^40]
+    bool fast = fast_div && bk <= 0x1p40f;  // then max_diag is 0 or in [2^-30, 2^40]
     const float sd = fast ? div_recip(max_diag, SQRT2_F, RCP_SQRT2_F) : max_diag / SQRT2_F;
     const float alph = poly_atanf(fmaxf(max_cross, sd));
     float sharp = 1.0f;
-    const float newsh = 1.0f + alph - c.Kalpha0;
+    const float newsh = 1.0f + alph - Kalpha;
     if (newsh > sharp) sharp = newsh;
     sharp *= sharp * sharp;
-    const float S = c.dt * c.Kspeed0 * sharp * H / 2.0f;  // a == L == 1
+    const float S = dt * Kspeed * sharp * H / 2.0f;  // a == L == 1
     fast = fast && S >= 0x1p-50f && S <= 0x1p40f;
     if (fast) {
         // S > 0: an unmarked direction's dividend S * 0 is +0 and its
@@ -407,6 +413,21 @@ __device__ __forceinline__ void cell_thermal_outflows(const StepConsts& c, float
         for (int k = 0; k < 8; ++k)
             if (dm[k] != 0.0f) o[k] = S * dh[k] / bk;
     }
+}
+
+// Layer 0 (rock): drops b - nb[k], H capped by b.
+__device__ __forceinline__ void cell_thermal_outflows(const StepConsts& c, float b, const float nb[8], float o[8]) {
+    float dh[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dh[k] = b - nb[k];
+    cell_thermal_outflows_dh(c.dt, c.Kalpha0, c.Kspeed0, c.talus_x_cross, c.talus_b_diag, c.fast_div, b, dh, o);
+}
+
+// Layer 1 (dirt) of a two-layer world: drops summed over rock and dirt,
+// (0 + (r - nr)) + (g - ng), H capped by the dirt height g.
+__device__ __forceinline__ void cell_thermal_outflows1(const StepConsts& c, const Talus1& t, const float dh[8],
+                                                       float g, float o[8]) {
+    cell_thermal_outflows_dh(c.dt, c.Kalpha1, c.Kspeed1, t.x_cross, t.b_diag, t.fast_div, g, dh, o);
 }
 
 // ---- thermal_transport (layer 0), glsl/thermal_transport.glsl:31-65 ----------------

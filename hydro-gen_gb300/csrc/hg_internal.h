@@ -76,6 +76,23 @@ struct RenderInput {
 int render_image(const RenderInput& in, const hg_camera& cam, int width, int height, uint8_t* rgba_dev,
                  float* rgb_dev, cudaStream_t st);
 
+// ---- fused two-layer step (hg_fused2.cu) ------------------------------------------
+// Inputs and outputs of one fused two-layer step (out of place) and its
+// scratch fields.
+struct Fused2Bufs {
+    const float *rock, *dirt, *water, *s0, *s1, *fl, *fr, *ft, *fb;
+    float *rock_o, *dirt_o, *water_o, *s0_o, *s1_o, *fl_o, *fr_o, *ft_o, *fb_o;
+    float *u, *v;
+    float *s0_ero, *s1_ero;  // eroded sediment (rock, dirt)
+    float *b_ero;            // eroded rock (input of the rock talus pass)
+    float *rock_mid;         // rock after the rock talus pass (input of the dirt pass)
+    float *g_ero;            // eroded dirt (input of the dirt pass)
+};
+struct TmaCache;
+bool fused2_ok(int n);
+int launch_fused2_step(const StepConsts& c, const Talus1& t1, const RainStep& r, const Fused2Bufs& b, TmaCache& tma,
+                       int* err, cudaStream_t st);
+
 // ---- particle erosion (hg_particles.cu) --------------------------------------------
 // Droplets as structure of arrays (Particle, glsl/bindings.glsl:101-110).
 struct Drops {

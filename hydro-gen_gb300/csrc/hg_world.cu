@@ -312,6 +312,17 @@ StepConsts make_consts(const hg_world* w) {
     return c;
 }
 
+Talus1 make_talus1(const hg_world* w) {
+    Talus1 t{};
+    t.x_cross = talus_cross_threshold(w->es.Kalpha[1]);
+    t.b_diag = talus_diag_threshold(t.x_cross);
+    const float tiny = std::numeric_limits<float>::denorm_min();
+    if (t.x_cross < tiny) t.x_cross = tiny;
+    if (t.b_diag < tiny) t.b_diag = tiny;
+    t.fast_div = !(t.x_cross < 0x1p-30f) && !(t.b_diag < 0x1p-30f);
+    return t;
+}
+
 RainStep make_rain(const hg_world* w, uint64_t step1) {
     RainStep r{};
     const hg_step_options& o = w->opt;
@@ -1177,6 +1188,46 @@ int hg_world_set_step(hg_world* w, uint64_t step) {
     return HG_OK;
 }
 
+namespace {
+// Fused steps of a two-layer world: three kernels per step (hg_fused2.cu);
+// the reference rain runs as its own kernel before the step it falls on.
+int fused2_steps(hg_world* w, int nsteps) {
+    if (!fused2_ok(w->n)) return fail(HG_ERR_UNSUPPORTED, "fused mode needs n divisible by 64");
+    const StepConsts c = make_consts(w);
+    const Talus1 t1 = make_talus1(w);
+    cudaStream_t st = w->stream;
+    const size_t cl = cells(w);
+    float* scratch = reinterpret_cast<float*>(w->tc);  // 4 n^2 floats
+    for (int k = 0; k < nsteps; ++k) {
+        const uint64_t step1 = w->step + 1;
+        RainStep r = make_rain(w, step1);
+        if (w->opt.rain_mode == HG_RAIN_REFERENCE) {
+            rain_pass(w, c, step1, w->cur[S_ROCK], w->dirt[0], w->cur[S_WATER], st);
+            r.active = 0;
+        }
+        Fused2Bufs b{};
+        b.rock = w->cur[S_ROCK]; b.dirt = w->dirt[0]; b.water = w->cur[S_WATER];
+        b.s0 = w->cur[S_SED]; b.s1 = w->sdirt[0];
+        b.fl = w->cur[S_FL]; b.fr = w->cur[S_FR]; b.ft = w->cur[S_FT]; b.fb = w->cur[S_FB];
+        b.rock_o = w->alt[S_ROCK]; b.dirt_o = w->dirt[1]; b.water_o = w->alt[S_WATER];
+        b.s0_o = w->alt[S_SED]; b.s1_o = w->sdirt[1];
+        b.fl_o = w->alt[S_FL]; b.fr_o = w->alt[S_FR]; b.ft_o = w->alt[S_FT]; b.fb_o = w->alt[S_FB];
+        b.u = w->u; b.v = w->v;
+        b.s0_ero = w->s_ero; b.s1_ero = scratch; b.b_ero = w->b_ero;
+        b.rock_mid = scratch + cl; b.g_ero = scratch + 2 * cl;
+        int rc = launch_fused2_step(c, t1, r, b, w->tma, w->err, st);
+        if (rc != HG_OK) return fail(rc, "cuTensorMapEncodeTiled failed for a world buffer");
+        for (int f = 0; f < S_COUNT; ++f) std::swap(w->cur[f], w->alt[f]);
+        std::swap(w->dirt[0], w->dirt[1]);
+        std::swap(w->sdirt[0], w->sdirt[1]);
+        w->step += 1;
+    }
+    w->dev_step_valid = false;
+    HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+}  // namespace
+
 int hg_step(hg_world* w, int nsteps, int mode) {
     HG_CHECK_WORLD(w);
     if (nsteps < 0) return fail(HG_ERR_INVALID, "nsteps must be >= 0");
@@ -1282,8 +1333,10 @@ int hg_step(hg_world* w, int nsteps, int mode) {
             w->step += 1;
         }
         if (nsteps > 0) w->dev_step_valid = false;
+    } else if (nsteps > 0 && w->layers == 2) {
+        int rc = fused2_steps(w, nsteps);
+        if (rc != HG_OK) return rc;
     } else if (nsteps > 0) {
-        if (w->layers != 1) return fail(HG_ERR_UNSUPPORTED, "the fused step covers one-layer worlds");
         std::vector<hg_world*> one{w};
         int rc = fused_run(w->plans, one, w->tuning, w->opt.tile_y, w->opt.graph, st, w->err, nsteps);
         if (rc != HG_OK) return rc;

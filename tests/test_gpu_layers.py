@@ -1,7 +1,8 @@
 """Two-layer worlds (rock + dirt, both sediment channels): the per-pass
-kernels against the float oracle's two-layer model, bit for bit, with the
-reference's default settings (Kconv, both slippage rates, smoothing) and with
-the config-2 rain; plus what the two-layer world does not support."""
+kernels and the fused three-kernel step against the float oracle's two-layer
+model, bit for bit, with the reference's default settings (Kconv, both
+slippage rates, smoothing) and with the config-2 rain; plus what the
+two-layer world does not support."""
 import numpy as np
 import pytest
 
@@ -68,10 +69,9 @@ def test_two_layer_limits_and_checkpoint(tmp_path):
     w.init_heightmap(H.noise(seed=1))
     w.upload("dirt", np.full((64, 64), 0.5, np.float32))
     w.step(5, H.MODE_PLAIN)
-    for bad in (lambda: w.step(1, H.MODE_FUSED), lambda: H.Tape(w, 4)):
-        with pytest.raises(H.HydrogenError) as e:
-            bad()
-        assert e.value.code == -5
+    with pytest.raises(H.HydrogenError) as e:
+        H.Tape(w, 4)
+    assert e.value.code == -5
     path = str(tmp_path / "w2.bin")
     w.save(path)
     v = H.World(64, layers=2)
@@ -85,3 +85,59 @@ def test_two_layer_limits_and_checkpoint(tmp_path):
         one.load(path)  # layer count differs
     with pytest.raises(H.HydrogenError):
         one.download("dirt")  # no dirt layer
+
+
+FUSED_FIELDS = ["rock", "dirt", "water", "sediment", "sediment_dirt", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u",
+                "vel_v"]
+
+
+def check_fused(w, ow, ctx):
+    for f in FUSED_FIELDS:
+        g, r = w.download(f).astype(np.float64), ow.get(f)
+        bad = np.argwhere(g != r)
+        assert bad.size == 0, f"{ctx} {f}: {len(bad)} cells differ, first {bad[:3].tolist()}"
+
+
+@pytest.mark.parametrize("case", ["defaults", "config2_rain", "no_dirt_talus", "rock_talus_off"])
+def test_two_layer_fused_bitwise_vs_float_oracle(case):
+    # 192 = 3 x 64: edge tiles on every side and interior tiles
+    n = 192
+    if case == "config2_rain":
+        s = H.settings_config2()
+        s.Kconv = 0.01
+        s.Kspeed[1] = 1.0
+        s.Kalpha[1] = 0.4
+        w, ow, os_, oo = make(n, s, H.rain_uniform(0.5, 1), H.options(H.RAIN_BERNOULLI, p=0.02, seed=9),
+                              O.options(2, 1, 0.5, p=0.02, seed=9), seed=1)
+        steps = 25
+    else:
+        s = reference_defaults()
+        if case == "no_dirt_talus":
+            s.Kspeed[1] = 0.0  # no dirt pass, no smoothing: two kernels per step
+        if case == "rock_talus_off":
+            s.Kspeed[0] = 0.0
+        w, ow, os_, oo = make(n, s, H.rain_uniform(0.01, 1), H.options(H.RAIN_UNIFORM), O.options(1, 1, 0.01))
+        steps = 30
+    for k in range(steps):
+        w.step(1, H.MODE_FUSED)
+        ow.step(os_, oo, 1)
+        if k in (0, 1, steps - 1):
+            check_fused(w, ow, f"{case} step {k + 1}")
+    assert np.any(w.download("sediment_dirt"))
+
+
+def test_two_layer_fused_matches_plain_with_reference_rain():
+    n = 128
+    ms = H.map_settings(hmap_dims=(n, n), max_height=64.0)
+    worlds = []
+    for mode in (H.MODE_PLAIN, H.MODE_FUSED):
+        w = H.World(n, layers=2)
+        w.init_reference_heightmap(ms)
+        w.set_erosion(reference_defaults())
+        w.set_rain(H.rain_uniform(0.2, 3))
+        w.set_options(H.options(H.RAIN_REFERENCE, time0=1.0, time_step=0.25))
+        w.step(20, mode)
+        worlds.append(w)
+    for f in FUSED_FIELDS:
+        assert np.array_equal(worlds[0].download(f), worlds[1].download(f)), f
+    assert worlds[0].step_count == worlds[1].step_count == 20
