@@ -1406,7 +1406,9 @@ int hg_batch_step(hg_batch* b, int nsteps, int mode) {
         return fail(HG_ERR_INVALID, "bad mode");
     if (nsteps == 0) return HG_OK;
     DeviceGuard g(b->device);
-    if (mode != HG_MODE_FUSED) {  // every world on its own stream, its own launches
+    bool two_layer = false;  // the table launch covers one-layer worlds
+    for (hg_world* w : b->worlds) two_layer = two_layer || w->layers == 2;
+    if (mode != HG_MODE_FUSED || two_layer) {  // every world on its own stream, its own launches
         for (hg_world* w : b->worlds) {
             int rc = hg_step(w, nsteps, mode == HG_MODE_PLAIN ? HG_MODE_PLAIN : HG_MODE_FUSED);
             if (rc != HG_OK) return rc;

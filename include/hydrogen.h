@@ -165,7 +165,7 @@ typedef struct hg_noise_settings {
 #define HG_FIELD_COUNT 15
 
 #define HG_MODE_PLAIN 0           /* one kernel per GLSL pass */
-#define HG_MODE_FUSED 1           /* two fused, tiled kernels per step */
+#define HG_MODE_FUSED 1           /* fused, tiled kernels: two per step (three in two-layer worlds) */
 #define HG_MODE_FUSED_PER_WORLD 2 /* batches only: each world's own fused launches */
 #define HG_MODE_PARTICLES 3       /* droplet erosion (hg_particles_init; two-layer worlds) */
 
@@ -193,10 +193,11 @@ int hg_default_step_options(hg_step_options* out);
  * src/erosion.cpp:83-84) on the current device.  layers 1: rock with an
  * empty dirt layer (Kconv and the dirt layer's terms vanish; every mode);
  * layers 2: the reference's rock + dirt model with both sediment channels
- * (HG_MODE_PLAIN only; fused steps, batches in fused mode and tapes need
- * layers 1).  All fields start at zero; the settings start at the
- * reference's defaults (src/state.cpp:81-92), with Kconv and Kspeed[1] at 0
- * for one-layer worlds. */
+ * (per-pass and fused steps, particle erosion; a batch of them in fused mode
+ * runs each world's own fused launches; tapes need layers 1).  All fields
+ * start at zero; the settings start at the reference's defaults
+ * (src/state.cpp:81-92), with Kconv and Kspeed[1] at 0 for one-layer
+ * worlds. */
 int hg_world_create(int n, int layers, hg_world** out);
 
 /* The reference's map defaults (src/settings.hpp:27-57) with seed 0 (the
