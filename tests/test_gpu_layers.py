@@ -141,3 +141,24 @@ def test_two_layer_fused_matches_plain_with_reference_rain():
     for f in FUSED_FIELDS:
         assert np.array_equal(worlds[0].download(f), worlds[1].download(f)), f
     assert worlds[0].step_count == worlds[1].step_count == 20
+
+
+def test_two_layer_batch_fused_runs_each_world():
+    ws, solo = [], []
+    for i, n in enumerate((64, 128)):
+        for group in (ws, solo):
+            w = H.World(n, layers=2)
+            w.init_heightmap(H.noise(seed=i))
+            w.upload("dirt", np.full((n, n), 0.5, np.float32))
+            w.set_erosion(reference_defaults())
+            w.set_rain(H.rain_uniform(0.01, 1))
+            w.set_options(H.options(H.RAIN_UNIFORM))
+            group.append(w)
+    b = H.Batch(ws)
+    b.step(6, H.MODE_FUSED)
+    b.sync()
+    for w in solo:
+        w.step(6, H.MODE_PLAIN)
+    for w, v in zip(ws, solo):
+        for f in FUSED_FIELDS:
+            assert np.array_equal(w.download(f), v.download(f)), f
