@@ -15,7 +15,10 @@
 // (src/erosion.cpp:158-200; glsl/hydro_flux.glsl, hydro_erosion.glsl,
 // sediment_transport.glsl, thermal_erosion.glsl, thermal_transport.glsl,
 // smoothing.glsl).  Per-cell arithmetic is the per-pass kernels' code, so
-// the fused step equals them bit for bit.
+// the fused step equals them bit for bit.  The particle step
+// (src/erosion.cpp:132-156) reuses the last two: the rock talus pass alone,
+// then the dirt talus pass with smoothing's particle branch (momentum fold,
+// water decay; glsl/smoothing.glsl:76-95).
 #include "hg_internal.h"
 #include "hg_tma.cuh"
 
@@ -169,6 +172,7 @@ __global__ void __launch_bounds__(NT) k2f_hydro(const __grid_constant__ HydroArg
 struct TransportArgs {
     CUtensorMap map_be;  // eroded rock, 72 x 20 boxes
     StepConsts c;
+    int sediment;        // 0: the rock talus pass alone (particle mode)
     const float *u, *v, *s0, *s1;  // velocity, eroded sediment (rock, dirt)
     float *s0_o, *s1_o;            // transported sediment
     float* rock_o;                 // rock after the layer-0 talus pass
@@ -212,6 +216,7 @@ __device__ __forceinline__ void transport_tile(const TransportArgs& a, float* be
     const int iy = tid / GPR, g = tid % GPR;
     const int x0 = tx0 + 4 * g, y = ty0 + iy;
     const size_t gi0 = (size_t)y * n + x0;
+    if (a.sediment) {
     const float4 u4 = __ldg(reinterpret_cast<const float4*>(a.u + gi0));
     const float4 v4 = __ldg(reinterpret_cast<const float4*>(a.v + gi0));
     // sediment_transport, both channels: one back-trace, two gathers
@@ -232,6 +237,7 @@ __device__ __forceinline__ void transport_tile(const TransportArgs& a, float* be
     }
     st4(a.s0_o + gi0, make_float4(sa[0], sa[1], sa[2], sa[3]));
     st4(a.s1_o + gi0, make_float4(sb[0], sb[1], sb[2], sb[3]));
+    }
     if (!c.thermal) return;
 
     bool ok = __syncthreads_and(mbar_wait(bar, 0));
@@ -364,6 +370,14 @@ struct Layer1Args {
     Talus1 t1;
     int thermal1;              // layer-1 talus pass on (Kspeed[1] != 0)
     float *rock_o, *dirt_o;
+    // particle mode: smoothing's particle branch (glsl/smoothing.glsl:76-95),
+    // per cell: momentum fold and water decay
+    int particle;
+    float count;               // droplets
+    const float* water;
+    float* water_o;
+    const float* mom[4];
+    float* mom_o[4];
 };
 
 // region (rx, ry) of the staged boxes <-> global (tx0 - HX + rx, ty0 - 3 + ry);
@@ -459,10 +473,37 @@ __device__ __forceinline__ void layer1_tile(const Layer1Args& a, float* R, float
         const int x = tx0 + ix, y = ty0 + iy;
         const int si = (3 + iy) * RW + HX + ix;
         float r = R[si], gg = Gd[si];
-        if (c.smooth_m != 0.0f && !(x == 0 || y == 0 || x == n - 1 || y == n - 1))
+        const bool border = x == 0 || y == 0 || x == n - 1 || y == n - 1;
+        const size_t gi = (size_t)y * n + x;
+        if (a.particle) {
+            // border texels copy their heights and water and leave the
+            // momentum map's write buffer as it was
+            float wat = a.water[gi];
+            if (!border) {
+                cell_smooth2(c.smooth_m, r, gg, R[si - 1], Gd[si - 1], R[si + 1], Gd[si + 1], R[si + RW],
+                             Gd[si + RW], R[si - RW], Gd[si - RW]);
+                float mx = a.mom[0][gi], my = a.mom[1][gi], mz = a.mom[2][gi], mw = a.mom[3][gi];
+                const float keep = gclamp(1.0f - 1e-12f * a.count, 0.0f, 1.0f);
+                mx *= keep;
+                my *= keep;
+                mx += 1e-12f * a.count * mz;
+                my += 1e-12f * a.count * mw;
+                wat *= gclamp(1.0f - 8e-8f * a.count, 0.0f, 1.0f);
+                if (wat < 1e-6f) wat = 0.0f;
+                if (sqrtf(mx * mx + my * my) < 1e-12f) {
+                    mx = 0.0f;
+                    my = 0.0f;
+                }
+                a.mom_o[0][gi] = mx;
+                a.mom_o[1][gi] = my;
+                a.mom_o[2][gi] = 0.0f;
+                a.mom_o[3][gi] = 0.0f;
+            }
+            a.water_o[gi] = wat;
+        } else if (c.smooth_m != 0.0f && !border) {
             cell_smooth2(c.smooth_m, r, gg, R[si - 1], Gd[si - 1], R[si + 1], Gd[si + 1], R[si + RW], Gd[si + RW],
                          R[si - RW], Gd[si - RW]);
-        const size_t gi = (size_t)y * n + x;
+        }
         a.rock_o[gi] = r;
         a.dirt_o[gi] = gg;
     }
@@ -517,6 +558,7 @@ int launch_fused2_step(const StepConsts& c, const Talus1& t1, const RainStep& r,
     TransportArgs ta{};
     if (l0 && !tma.get(b.b_ero, n, T_RH, &ta.map_be)) return HG_ERR_CUDA;
     ta.c = c;
+    ta.sediment = 1;
     ta.u = b.u; ta.v = b.v;
     ta.s0 = b.s0_ero; ta.s1 = b.s1_ero;
     ta.s0_o = b.s0_o; ta.s1_o = b.s1_o;
@@ -532,14 +574,47 @@ int launch_fused2_step(const StepConsts& c, const Talus1& t1, const RainStep& r,
         la.thermal1 = c.Kspeed1 != 0.0f ? 1 : 0;
         la.rock_o = b.rock_o;
         la.dirt_o = b.dirt_o;
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k2f_layer1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LAYER1_SMEM);
-            attr = true;
-        }
+        // per device and cheap: set on every launch rather than cached
+        cudaFuncSetAttribute(k2f_layer1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LAYER1_SMEM);
         k2f_layer1<<<tiles, NT, LAYER1_SMEM, st>>>(la, err);
         count_launch();
     }
+    return HG_OK;
+}
+
+int launch_particle_thermal_smooth(const StepConsts& c, const Talus1& t1, float count, const PWorld& in,
+                                   const PWorld& out, float* rock_mid, TmaCache& tma, int* err, cudaStream_t st) {
+    const int n = c.n;
+    const int tiles = (n / TW) * (n / TH);
+    const float* rock_l0 = in.rock;
+    if (c.thermal) {  // the rock talus pass alone
+        TransportArgs ta{};
+        if (!tma.get(in.rock, n, T_RH, &ta.map_be)) return HG_ERR_CUDA;
+        ta.c = c;
+        ta.sediment = 0;
+        ta.rock_o = rock_mid;
+        k2f_transport<<<tiles, NT, 0, st>>>(ta, err);
+        count_launch();
+        rock_l0 = rock_mid;
+    }
+    Layer1Args la{};
+    if (!tma.get(rock_l0, n, L_RH, &la.map_r) || !tma.get(in.dirt, n, L_RH, &la.map_g)) return HG_ERR_CUDA;
+    la.c = c;
+    la.t1 = t1;
+    la.thermal1 = c.Kspeed1 != 0.0f ? 1 : 0;
+    la.rock_o = out.rock;
+    la.dirt_o = out.dirt;
+    la.particle = 1;
+    la.count = count;
+    la.water = in.water;
+    la.water_o = out.water;
+    for (int k = 0; k < 4; ++k) {
+        la.mom[k] = in.mom[k];
+        la.mom_o[k] = out.mom[k];
+    }
+    cudaFuncSetAttribute(k2f_layer1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LAYER1_SMEM);
+    k2f_layer1<<<tiles, NT, LAYER1_SMEM, st>>>(la, err);
+    count_launch();
     return HG_OK;
 }
 

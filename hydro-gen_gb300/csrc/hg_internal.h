@@ -131,6 +131,13 @@ void launch_particle_step(const StepConsts& c, const hg_erosion_settings& es, co
                           const PWorld& pw, uint32_t step1, uint64_t seed, bool should_rain, cudaStream_t st);
 // smoothing with the particle branch: in -> out (all of rock, dirt, water, momentum)
 void launch_particle_smooth(const StepConsts& c, float count, const PWorld& in, const PWorld& out, cudaStream_t st);
+struct TmaCache;
+struct Talus1;
+// the particle step's talus passes (rock, then dirt) and smoothing with the
+// particle branch as fused kernels (hg_fused2.cu, n a multiple of 64):
+// in -> out, the rock after its talus pass in rock_mid
+int launch_particle_thermal_smooth(const StepConsts& c, const Talus1& t1, float count, const PWorld& in,
+                                   const PWorld& out, float* rock_mid, TmaCache& tma, int* err, cudaStream_t st);
 
 // ---- fused step (hg_fused.cu) ---------------------------------------------------
 // Rain settings without the step number (the kernels add the step).

@@ -1243,11 +1243,25 @@ int hg_step(hg_world* w, int nsteps, int mode) {
         // the momentum fold; rain on = new droplets spawn
         if (!w->parts) return fail(HG_ERR_INVALID, "particle mode needs hg_particles_init");
         Particles& P = *w->parts;
+        const Talus1 t1 = make_talus1(w);
         auto swap2 = [](float** f) { float* t = f[0]; f[0] = f[1]; f[1] = t; };
         for (int k = 0; k < nsteps; ++k) {
             PWorld cur{w->cur[S_ROCK], w->dirt[0], w->cur[S_WATER], {P.mom[0][0], P.mom[0][1], P.mom[0][2], P.mom[0][3]}};
             launch_particle_step(c, w->es, P.b, cur, (uint32_t)(w->step + 1), w->opt.rain_seed,
                                  w->opt.rain_mode != HG_RAIN_OFF, st);
+            if (fused2_ok(w->n)) {  // talus passes and smoothing as fused kernels
+                PWorld out{w->alt[S_ROCK], w->dirt[1], w->alt[S_WATER],
+                           {P.mom[1][0], P.mom[1][1], P.mom[1][2], P.mom[1][3]}};
+                float* rock_mid = reinterpret_cast<float*>(w->tc);
+                int rc = launch_particle_thermal_smooth(c, t1, (float)P.count, cur, out, rock_mid, w->tma, w->err, st);
+                if (rc != HG_OK) return fail(rc, "cuTensorMapEncodeTiled failed for a world buffer");
+                swap(S_ROCK);
+                swap(S_WATER);
+                swap2(w->dirt);
+                for (int ch = 0; ch < 4; ++ch) std::swap(P.mom[0][ch], P.mom[1][ch]);
+                w->step += 1;
+                continue;
+            }
             if (c.thermal) {
                 launch_thermal_out(c, w->cur[S_ROCK], w->tc, w->td, st);
                 launch_thermal_in(c, w->cur[S_ROCK], w->tc, w->td, w->alt[S_ROCK], st);
