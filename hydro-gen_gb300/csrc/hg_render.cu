@@ -430,8 +430,10 @@ __device__ __forceinline__ unsigned char unorm8(float f) {
     return (unsigned char)floorf(f * 255.0f + 0.5f);
 }
 
-// main (:525-539) and get_pixel_color (:393-460)
-__global__ void __launch_bounds__(128) k_render(const RenderArgs a) {
+// main (:525-539) and get_pixel_color (:393-460).  Eight blocks per SM (a
+// 64-register cap with small spills) hide the marches' latencies better
+// than five unspilled ones (9 % faster).
+__global__ void __launch_bounds__(128, 8) k_render(const RenderArgs a) {
     const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
     if (px >= a.wd || py >= a.hd) return;
     const Scene S = a.S;
