@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=N_GRID)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
-    ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain"], default=None,
+    ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint"], default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
     return ap.parse_args()
@@ -591,6 +591,9 @@ def main():
                 out = bench_two_layer(H, torch, nsteps=args.steps, warmup=args.warmup, cpu_budget_s=budget)
             elif args.extra == "terrain":
                 out = bench_terrain(H, torch, reps=args.steps, cpu_budget_s=budget)
+            elif args.extra == "adjoint":  # --steps reversed steps, --warmup timed repetitions
+                out = bench_adjoint(H, torch, nsteps=args.steps, ckpt=min(32, args.steps),
+                                    reps=max(1, args.warmup))
             else:
                 out = bench_render(H, torch, frames=args.steps, warmup=args.warmup, cpu_budget_s=budget)
             print(json.dumps(out), flush=True)
