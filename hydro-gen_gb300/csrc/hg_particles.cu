@@ -255,7 +255,7 @@ struct ApplyArgs {
     Drops d;
     int n;
     const uint32_t* offs;  // n*n + 1
-    const uint32_t* keys;  // records bucketed by texel, any order within a bucket
+    uint32_t* keys;        // records bucketed by texel, any order within a bucket
     uint32_t* sorted;      // big texels: their bucket in droplet-id order
     uint32_t* hot;         // [0], [1]: mid and big texel counts; then mid texels
                            // from [2], big texels from [2 + hot_cap]
@@ -541,9 +541,9 @@ __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_mid(const ApplyArgs a
 }
 
 // one warp per big texel (more than 32 records): sort the bucket by droplet
-// id (bitonic network in shared memory; buckets above HOT_KEYS by rank
-// counting over global memory), then stage 32 records at a time in shared
-// memory for lane 0's sequential update
+// id (bitonic network in shared memory, chunks of HOT_KEYS merged by rank),
+// then stage 32 prepared records at a time in shared memory for lane 0's
+// sequential update
 __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_big(const ApplyArgs a) {
     __shared__ uint32_t sk[HOT_WARPS][HOT_KEYS];
     __shared__ Rec sr[HOT_WARPS][32];
@@ -553,10 +553,15 @@ __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_big(const ApplyArgs a
     for (uint32_t h = blockIdx.x * HOT_WARPS + wl; h < nbig; h += gridDim.x * HOT_WARPS) {
         const size_t t = a.hot[2 + a.hot_cap + h];
         const uint32_t lo = a.offs[t], hi = a.offs[t + 1], k = hi - lo;
-        if (k <= (uint32_t)HOT_KEYS) {
+        // sort chunks of up to HOT_KEYS records in shared memory into
+        // `sorted`; a bucket of several chunks is then merged into `keys` by
+        // each record's rank (its place in its chunk plus, per other chunk,
+        // the records below it found by binary search)
+        for (uint32_t c0 = 0; c0 < k; c0 += HOT_KEYS) {
+            const uint32_t len = min((uint32_t)HOT_KEYS, k - c0);
             uint32_t P = 32;
-            while (P < k) P <<= 1;
-            for (uint32_t i = lane; i < P; i += 32) sk[wl][i] = i < k ? a.keys[lo + i] : 0xffffffffu;
+            while (P < len) P <<= 1;
+            for (uint32_t i = lane; i < P; i += 32) sk[wl][i] = i < len ? a.keys[lo + c0 + i] : 0xffffffffu;
             __syncwarp();
             for (uint32_t size = 2; size <= P; size <<= 1)
                 for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
@@ -571,21 +576,35 @@ __global__ void __launch_bounds__(32 * HOT_WARPS) k_papply_big(const ApplyArgs a
                     }
                     __syncwarp();
                 }
-            for (uint32_t i = lane; i < k; i += 32) a.sorted[lo + i] = sk[wl][i];
-        } else {
+            for (uint32_t i = lane; i < len; i += 32) a.sorted[lo + c0 + i] = sk[wl][i];
+            __syncwarp();
+        }
+        const bool merged = k > (uint32_t)HOT_KEYS;
+        if (merged) {
             for (uint32_t i = lane; i < k; i += 32) {
-                const uint32_t key = a.keys[lo + i];
-                uint32_t rank = 0;
-                for (uint32_t j = 0; j < k; ++j) rank += a.keys[lo + j] < key ? 1u : 0u;
-                a.sorted[lo + rank] = key;
+                const uint32_t key = a.sorted[lo + i];
+                const uint32_t own = i / HOT_KEYS * HOT_KEYS;
+                uint32_t rank = i - own;
+                for (uint32_t c0 = 0; c0 < k; c0 += HOT_KEYS) {
+                    if (c0 == own) continue;
+                    uint32_t l = 0, h = min((uint32_t)HOT_KEYS, k - c0);  // records of chunk c0 below key
+                    const uint32_t* ch = a.sorted + lo + c0;
+                    while (l < h) {
+                        const uint32_t m = (l + h) >> 1;
+                        if (ch[m] < key) l = m + 1; else h = m;
+                    }
+                    rank += l;
+                }
+                a.keys[lo + rank] = key;
             }
         }
+        const uint32_t* order = merged ? a.keys : a.sorted;
         __syncwarp();
         Texel T = load_texel(a, t);
         for (uint32_t base = lo; base < hi; base += 32) {
             const uint32_t m = min(32u, hi - base);
             if ((uint32_t)lane < m) {
-                const Rec r = load_rec(a, a.sorted[base + lane]);
+                const Rec r = load_rec(a, order[base + lane]);
                 sr[wl][lane] = r;
                 sp[wl][lane] = prep_record(a, r);
             }

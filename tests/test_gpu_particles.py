@@ -71,13 +71,15 @@ def test_particles_crowded_texels_and_kills():
     assert it.max() <= 6
 
 
-def test_particles_pile_up_beyond_shared_sort():
-    # 16384 droplets on an 8x8 map: every live droplet sits on the same few
-    # texels, buckets of thousands of records (above the 2048 a warp sorts in
-    # shared memory)
+@pytest.mark.parametrize("count", [16384, 65536])
+def test_particles_pile_up_beyond_shared_sort(count):
+    # thousands of droplets on an 8x8 map: every live droplet sits on the
+    # same few texels, buckets of thousands to tens of thousands of records
+    # (several of the 2048-record chunks a warp sorts in shared memory,
+    # merged by rank)
     s = H.settings_particles()
     s.Kspeed[0] = 0.0
-    w, ow, os_, oo = make(8, 16384, s, seed=5)
+    w, ow, os_, oo = make(8, count, s, seed=5)
     for k in range(3):
         w.step(1, H.MODE_PARTICLES)
         ow.particle_step(os_, oo, 1)
