@@ -1007,6 +1007,22 @@ int hg_render(hg_world* w, const hg_camera* cam, int width, int height, uint8_t*
     return HG_OK;
 }
 
+int hg_rain(hg_world* w, float time) {
+    HG_CHECK_WORLD(w);
+    DeviceGuard g(w->device);
+    if (w->opt.rain_mode == HG_RAIN_OFF) return HG_OK;
+    if (w->opt.rain_mode == HG_RAIN_REFERENCE) {
+        launch_ref_rain(w->rs, w->map, time, w->n, w->cur[S_ROCK], w->layers == 2 ? w->dirt[0] : nullptr,
+                        w->cur[S_WATER], w->stream);
+    } else {
+        RainStep r = make_rain(w, w->step + 1);
+        r.active = 1;
+        launch_rain(make_consts(w), r, w->cur[S_WATER], w->stream);
+    }
+    HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+
 int hg_particles_init(hg_world* w, int count) {
     HG_CHECK_WORLD(w);
     if (w->layers != 2) return fail(HG_ERR_UNSUPPORTED, "particle erosion runs on two-layer worlds");

@@ -132,6 +132,7 @@ def _load():
         "hg_set_map_settings": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
         "hg_init_reference_heightmap": (ctypes.c_int, [P, ctypes.POINTER(MapSettings)]),
         "hg_particles_init": (ctypes.c_int, [P, ctypes.c_int]),
+        "hg_rain": (ctypes.c_int, [P, ctypes.c_float]),
         "hg_camera_look_at": (ctypes.c_int, [ctypes.POINTER(Camera), P, P, P, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_float, ctypes.c_float]),
         "hg_render": (ctypes.c_int, [P, ctypes.POINTER(Camera), ctypes.c_int, ctypes.c_int, P, P]),
@@ -370,6 +371,10 @@ class World:
 
     def step(self, nsteps=1, mode=MODE_PLAIN):
         check(lib.hg_step(self.h, nsteps, mode))
+
+    def rain(self, time=0.0):
+        """One rain pass now (Erosion::dispatch_grid_rain), whatever the period."""
+        check(lib.hg_rain(self.h, time))
 
     def sync(self):
         check(lib.hg_sync(self.h))

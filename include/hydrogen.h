@@ -315,6 +315,14 @@ int hg_world_set_step(hg_world* w, uint64_t step);
  * thermal_erosion/thermal_transport.  mode selects the per-pass kernels or
  * the fused kernel; both give bit-identical fields.  Asynchronous. */
 int hg_step(hg_world* w, int nsteps, int mode);
+/* Replaces Erosion::dispatch_grid_rain (src/erosion.cpp:76-89) for callers
+ * that keep the reference's own cadence (src/main.cpp:315-319): one rain
+ * pass now, whatever the rain period, with the world's rain model
+ * (HG_RAIN_REFERENCE at frame time `time`; uniform and Bernoulli rain keyed
+ * by the next step number; nothing when HG_RAIN_OFF).  The step counter does
+ * not advance.  Such a caller steps with rain_mode's own cadence disabled
+ * (period 0), so hg_step adds no rain of its own.  Asynchronous. */
+int hg_rain(hg_world* w, float time);
 /* Waits for the world's stream (the reference's glMemoryBarrier/glFinish).
  * HG_ERR_TIMEOUT if a fused-step tile load gave up its bounded wait since the
  * last sync (the step's fields are then not valid). */

@@ -78,3 +78,22 @@ def test_reference_rain_fused_equals_plain():
     b.step(13, H.MODE_FUSED)  # rain on steps 3, 6, 9, 12 inserted before the fused launches
     for f in H.STATE_FIELDS:
         assert np.array_equal(a.download(f), b.download(f)), f
+
+
+def test_standalone_rain_pass_matches_the_restatement():
+    # hg_rain is Erosion::dispatch_grid_rain: one pass at the given frame
+    # time, whatever the period; water starts at 0, so it holds the increment
+    n = 128
+    w = H.World(n, layers=2)
+    ms = H.map_settings(hmap_dims=(n, n), max_height=64.0)
+    w.init_reference_heightmap(ms)
+    r = H.rain_uniform(0.02, 0)
+    r.mountain_thresh, r.mountain_multip, r.drops = 0.3, 0.05, 0.05
+    w.set_rain(r)
+    w.set_options(H.options(H.RAIN_REFERENCE))
+    w.rain(2.5)
+    total = (w.download("rock") + w.download("dirt")).astype(np.float32)
+    expect = O.ref_rain(total, 2.5, r, 64.0)
+    assert np.array_equal(w.download("water"), expect)
+    assert w.step_count == 0 and np.any(expect > 0)
+    w.step(2, H.MODE_PLAIN)  # period 0: the step adds no rain of its own
