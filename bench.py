@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_GRID)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
-    ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint"], default=None,
+    ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint", "config1"],
+                    default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
     return ap.parse_args()
@@ -298,7 +299,46 @@ def bench_large(H, torch, n=8192, fwd_steps=2000, adj_steps=512, nbatch=16, bn=1
     return out
 
 
-def bench_batch(H, torch, count=64, nsteps=50, warmup=16):
+def bench_config1(H, torch, n=256, nsteps=1000, reps=3, cpu=True):
+    """Config 1 as the workloads define it: 256^2, uniform rain 0.01 every
+    step, thermal off, 1000 steps; per-pass and fused kernels (CUDA events,
+    median of three runs), and the float and FP64 oracles on the host."""
+    out = {"workload": f"config1 {n}x{n}, {nsteps} steps", "steps": nsteps}
+    for name, mode in (("plain", H.MODE_PLAIN), ("fused", H.MODE_FUSED)):
+        times = []
+        for r in range(reps + 1):
+            w = H.World(n)
+            w.init_heightmap(H.noise(seed=0))
+            H.configure(w, "config1")
+            w.sync()
+            stream = torch.cuda.ExternalStream(w.stream)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            w.step(nsteps, mode)
+            e1.record(stream)
+            e1.synchronize()
+            if r:
+                times.append(e0.elapsed_time(e1))
+            w.close()
+        ms = statistics.median(times)
+        out[name] = {"ms_per_run": ms, "cell_steps_per_s": n * n * nsteps / (ms / 1e3)}
+    if not cpu:
+        return out
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    s, o = O.workload("config1")
+    for prec in (32, 64):
+        ow = O.OracleWorld(n, prec)
+        ow.set("rock", O.fbm(n))
+        t0 = time.perf_counter()
+        ow.step(s, o, nsteps)
+        el = time.perf_counter() - t0
+        out[f"cpu_fp{prec}"] = {"value": n * n * nsteps / el, "unit": "cell-steps/s", "cores": O.num_threads(),
+                                "kind": "port", "sample": f"the full run, {el:.2f} s"}
+    return out
+
+
+def bench_batch(H, torch, count=64, nsteps=200, warmup=16):
     """64 terrains of sides drawn from {256, 512, 1024, 2048} with their own
     seeds and parameters, stepped three ways: each terrain's own fused
     launches, one table launch per kernel for all terrains (tile height and
@@ -591,6 +631,8 @@ def main():
                 out = bench_two_layer(H, torch, nsteps=args.steps, warmup=args.warmup, cpu_budget_s=budget)
             elif args.extra == "terrain":
                 out = bench_terrain(H, torch, reps=args.steps, cpu_budget_s=budget)
+            elif args.extra == "config1":
+                out = bench_config1(H, torch, cpu=budget > 0)
             elif args.extra == "adjoint":  # --steps reversed steps, --warmup timed repetitions
                 out = bench_adjoint(H, torch, nsteps=args.steps, ckpt=min(32, args.steps),
                                     reps=max(1, args.warmup))
@@ -697,6 +739,7 @@ def main():
     if not args.no_extras:
         line["fwd_adjoint"] = bench_adjoint(H, torch)
         line["batch"] = bench_batch(H, torch)
+        line["config1"] = bench_config1(H, torch, cpu=not args.no_cpu_baseline)
         line["large"] = bench_large(H, torch)
         line["two_layer"] = bench_two_layer(H, torch)
         line["terrain"] = bench_terrain(H, torch)
