@@ -736,16 +736,20 @@ def main():
         "e2e": {"value": job_throughput(world_size, cells, args.steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
     }
-    if not args.no_extras:
+    # the extras and the CPU baseline are single-GPU measurements: the N = 1
+    # line carries them, replica lines (N > 1) do not hold N GPUs for them
+    single = world_size == 1
+    cpu = 0.0 if args.no_cpu_baseline else 6.0
+    if not args.no_extras and single:
         line["fwd_adjoint"] = bench_adjoint(H, torch)
         line["batch"] = bench_batch(H, torch)
-        line["config1"] = bench_config1(H, torch, cpu=not args.no_cpu_baseline)
+        line["config1"] = bench_config1(H, torch, cpu=cpu > 0)
         line["large"] = bench_large(H, torch)
-        line["two_layer"] = bench_two_layer(H, torch)
-        line["terrain"] = bench_terrain(H, torch)
-        line["particles"] = bench_particles(H, torch)
-        line["render"] = bench_render(H, torch)
-    if not args.no_cpu_baseline:
+        line["two_layer"] = bench_two_layer(H, torch, cpu_budget_s=cpu)
+        line["terrain"] = bench_terrain(H, torch, cpu_budget_s=cpu * 2.0 / 3.0)
+        line["particles"] = bench_particles(H, torch, cpu_budget_s=cpu)
+        line["render"] = bench_render(H, torch, cpu_budget_s=cpu)
+    if not args.no_cpu_baseline and single:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)
     if dist is not None:
