@@ -1937,6 +1937,10 @@ struct CkptHeader {
     hg_step_options opt;
 };
 const char kCkptMagic[8] = {'H', 'G', 'W', 'O', 'R', 'L', 'D', '1'};
+// optional trailer of a particle-mode world: magic, droplet count, the
+// droplet arrays (x, y, vx, vy, volume, two sediments, capacity, age, kill),
+// then the momentum map's x and y (its z and w are 0 between steps)
+const char kPartsMagic[8] = {'H', 'G', 'P', 'A', 'R', 'T', 'S', '1'};
 // the nine carried fields, then dirt and dirt sediment (two-layer worlds),
 // then the per-cell Ks field when set
 std::vector<int> ckpt_fields(int layers, bool ks_on) {
@@ -1981,6 +1985,30 @@ int hg_world_save(hg_world* w, const char* path) {
         }
         ok = std::fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
     }
+    if (ok && w->parts) {  // particle mode: droplets and the momentum map's x, y
+        const Drops& d = w->parts->b.d;
+        const int32_t count = d.count;
+        ok = std::fwrite(kPartsMagic, 8, 1, f) == 1 && std::fwrite(&count, sizeof(count), 1, f) == 1;
+        std::vector<uint32_t> col((size_t)count);
+        const void* arrays[10] = {d.px, d.py, d.vx, d.vy, d.vol, d.s0, d.s1, d.sc, d.iters, d.kill};
+        for (int k = 0; ok && k < 10; ++k) {
+            cudaError_t e = cudaMemcpy(col.data(), arrays[k], col.size() * 4, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) {
+                std::fclose(f);
+                return cuda_fail(e, "checkpoint download");
+            }
+            ok = std::fwrite(col.data(), 4, col.size(), f) == col.size();
+        }
+        for (int k = 0; ok && k < 2; ++k) {
+            cudaError_t e =
+                cudaMemcpy(buf.data(), w->parts->mom[0][k], buf.size() * sizeof(float), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) {
+                std::fclose(f);
+                return cuda_fail(e, "checkpoint download");
+            }
+            ok = std::fwrite(buf.data(), sizeof(float), buf.size(), f) == buf.size();
+        }
+    }
     ok = (std::fclose(f) == 0) && ok;
     if (!ok) return fail(HG_ERR_IO, std::string("write failed: ") + path);
     return HG_OK;
@@ -2015,6 +2043,41 @@ int hg_world_load(hg_world* w, const char* path) {
         }
         HG_CUDA(cudaMemcpyAsync(field_ptr(w, field), buf.data(), buf.size() * sizeof(float), cudaMemcpyHostToDevice,
                                 w->stream));
+        HG_CUDA(cudaStreamSynchronize(w->stream));
+    }
+    char tail[8];
+    if (std::fread(tail, 8, 1, f) == 1) {
+        int32_t count = 0;
+        if (std::memcmp(tail, kPartsMagic, 8) != 0 || std::fread(&count, sizeof(count), 1, f) != 1 || count < 1) {
+            std::fclose(f);
+            return fail(HG_ERR_IO, std::string("unknown data after the fields: ") + path);
+        }
+        if (!w->parts || w->parts->count != count) {
+            int rc = hg_particles_init(w, count);
+            if (rc != HG_OK) {
+                std::fclose(f);
+                return rc;
+            }
+        }
+        const Drops& d = w->parts->b.d;
+        std::vector<uint32_t> col((size_t)count);
+        void* arrays[10] = {d.px, d.py, d.vx, d.vy, d.vol, d.s0, d.s1, d.sc, d.iters, d.kill};
+        for (int k = 0; k < 12; ++k) {
+            const bool field = k >= 10;
+            void* dst = field ? (void*)w->parts->mom[0][k - 10] : arrays[k];
+            const size_t words = field ? buf.size() : col.size();
+            void* src = field ? (void*)buf.data() : (void*)col.data();
+            if (std::fread(src, 4, words, f) != words) {
+                std::fclose(f);
+                return fail(HG_ERR_IO, std::string("truncated checkpoint: ") + path);
+            }
+            HG_CUDA(cudaMemcpyAsync(dst, src, words * 4, cudaMemcpyHostToDevice, w->stream));
+            HG_CUDA(cudaStreamSynchronize(w->stream));
+        }
+        for (int k = 2; k < 4; ++k) {
+            HG_CUDA(cudaMemsetAsync(w->parts->mom[0][k], 0, buf.size() * sizeof(float), w->stream));
+        }
+        for (int k = 0; k < 4; ++k) HG_CUDA(cudaMemsetAsync(w->parts->mom[1][k], 0, buf.size() * sizeof(float), w->stream));
         HG_CUDA(cudaStreamSynchronize(w->stream));
     }
     std::fclose(f);

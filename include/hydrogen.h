@@ -392,13 +392,16 @@ int hg_mse(hg_world* w, const float* target, double* loss, float* dL_drock);
 
 /* ---- checkpoint / resume ------------------------------------------------------------ */
 /* No counterpart in the reference (its state lives only in GL textures).
- * Writes the carried fields (rock, water, sediment, four fluxes, u, v, and
- * the per-cell solubility when set), the step counter, the erosion and rain
- * settings and the step options to `path` (a fixed binary header, then
- * little-endian FP32 fields).  Resuming with hg_world_load and stepping reproduces an
- * uninterrupted run bit for bit (rain is keyed by the step counter).
- * Synchronises.  HG_ERR_IO on file errors, HG_ERR_INVALID if the file's
- * world size or layer count differs from w's. */
+ * Writes the carried fields (rock, water, sediment, four fluxes, u, v; dirt
+ * and dirt sediment in two-layer worlds; the per-cell solubility when set),
+ * the step counter, the erosion and rain settings and the step options to
+ * `path` (a fixed binary header, then little-endian FP32 fields), and in
+ * particle mode the droplets and the momentum map.  Resuming with
+ * hg_world_load (which sets up the droplets when the file has them) and
+ * stepping reproduces an uninterrupted run bit for bit (rain and droplet
+ * spawns are keyed by the step counter).  Synchronises.  HG_ERR_IO on file
+ * errors, HG_ERR_INVALID if the file's world size or layer count differs
+ * from w's. */
 int hg_world_save(hg_world* w, const char* path);
 int hg_world_load(hg_world* w, const char* path);
 

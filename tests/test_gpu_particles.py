@@ -109,3 +109,21 @@ def test_particles_rain_off_keeps_idle_and_limits():
     s.particle_count = 255
     with pytest.raises(H.HydrogenError):
         w.set_erosion(s)
+
+
+def test_particles_checkpoint_resume_is_bitwise(tmp_path):
+    s = H.settings_particles()
+    a, _, _, _ = make(64, 512, s, seed=3)
+    a.step(10, H.MODE_PARTICLES)
+    path = str(tmp_path / "p.bin")
+    a.save(path)
+    a.step(12, H.MODE_PARTICLES)
+    b = H.World(64, layers=2)
+    b.load(path)  # sets up the droplets from the file
+    b.step(12, H.MODE_PARTICLES)
+    sa, ia, ka = a.particles()
+    sb, ib, kb = b.particles()
+    assert np.array_equal(sa.view(np.uint32), sb.view(np.uint32)) and np.array_equal(ia, ib)
+    assert np.array_equal(ka, kb)
+    for f in ("rock", "dirt", "water", "momentum_x", "momentum_y"):
+        assert np.array_equal(a.download(f), b.download(f)), f
