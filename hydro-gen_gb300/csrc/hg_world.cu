@@ -142,6 +142,8 @@ struct Plan {
     BatchParams* bp[2] = {};            // batch launches: terrain records (kernel parameter)
     CUtensorMap* d_maps[2] = {};        // batch launches: tensor maps in device memory
     std::vector<std::array<const float*, S_COUNT>> key_cur, key_alt;  // buffers at build time
+    std::vector<float*> smooth_dst[2];  // per direction and world: the step's rock output when smoothing runs
+                                        // (the fused kernels then leave their rock in the world's scratch)
     std::vector<uint64_t> versions;
     cudaGraphExec_t graph[2] = {};  // two steps starting with table 0 / table 1
     uint64_t graph_launches = 4;    // kernel launches in one graph
@@ -404,6 +406,12 @@ int build_plan(Plan* p) {
             s.s_ero = w->s_ero;
             s.b_ero = w->b_ero;
             s.step = w->d_step;
+            p->smooth_dst[dir].resize(nt);
+            p->smooth_dst[dir][i] = nullptr;
+            if (s.c.smooth_m != 0.0f) {  // smoothing reads the fused rock from scratch into the real output
+                p->smooth_dst[dir][i] = s.out[S_ROCK];
+                s.out[S_ROCK] = reinterpret_cast<float*>(w->tc);
+            }
             if (!fill_desc(tab[i], s, p->th, tile0[i], w->tma))
                 return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a world buffer");
         }
@@ -463,16 +471,13 @@ int plan_dir(const Plan* p) {
 void launch_dir(Plan* p, int dir) {
     if (p->worlds.size() == 1) launch_fused_one(p->h_tab[dir][0], p->th, p->err, p->stream);
     else launch_fused_table(*p->bp[dir], p->d_maps[dir], p->total, p->th, p->err, p->stream);
-    // smoothing (worlds with Kspeed[1] != 0): the fused step's rock through
-    // the per-pass smoothing kernel into scratch (the per-pass thermal
-    // buffer) and back
+    // smoothing (worlds with Kspeed[1] != 0): the fused kernels left the
+    // step's rock in scratch (the per-pass thermal buffer); the per-pass
+    // smoothing kernel writes it into the step's rock output
     for (size_t i = 0; i < p->worlds.size(); ++i) {
         const TerrainHot& h = p->h_tab[dir][i].h;
         if (h.c.smooth_m == 0.0f) continue;
-        hg_world* w = p->worlds[i];
-        float* scratch = reinterpret_cast<float*>(w->tc);
-        launch_smooth(h.c, h.out[S_ROCK], scratch, p->stream);
-        cudaMemcpyAsync(h.out[S_ROCK], scratch, cells(w) * sizeof(float), cudaMemcpyDeviceToDevice, p->stream);
+        launch_smooth(h.c, h.out[S_ROCK], p->smooth_dst[dir][i], p->stream);
     }
 }
 

@@ -28,6 +28,12 @@ def make(ts, p=0.02, **opt):
             s = w.get_erosion()
             s.Kspeed[0] = 0.0
             w.set_erosion(s)
+        if i in (2, 4):  # two worlds with smoothing (Kspeed[1] != 0), one of them without thermal
+            s = w.get_erosion()
+            s.Kspeed[1] = 3.0
+            if i == 4:
+                s.Kspeed[0] = 0.0
+            w.set_erosion(s)
         ws.append(w)
     return ws
 
