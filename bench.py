@@ -160,10 +160,11 @@ def cpu_baseline(n_sample=1024, budget_s=12.0):
                       f"(float oracle, OpenMP over rows)"}
 
 
-def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3):
+def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fit_iters=8):
     """Forward + adjoint of the inverse-erosion workload: 1024^2, config-1
     physics, per-cell Ks = 0.05 exp(0.5 n(x)) from 3-octave simplex noise,
-    MSE to a target, gradients for Ks and the initial rock."""
+    MSE to a target, gradients for Ks and the initial rock; then fit_iters
+    iterations of the native descent (hg_inverse_fit) on both."""
     w = H.World(n)
     w.init_heightmap(H.noise(seed=0))
     H.configure(w, "config1")
@@ -201,9 +202,20 @@ def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3):
             all_ms.append(e0.elapsed_time(e2))
     f, a = statistics.median(fwd_ms), statistics.median(all_ms)
     cs = n * n * nsteps
+    # the fit itself, through hg_inverse_fit from uniform Ks = 0.05 and the
+    # true initial rock: wall time of the whole call (tape and scratch set-up included)
+    ks = torch.full((n, n), 0.05, dtype=torch.float32, device="cuda")
+    b0_dev = torch.from_numpy(b0).cuda()
+    fs = H.fit_settings(nsteps=nsteps, ckpt_every=ckpt, iters=fit_iters, ks_step=0.01, rock_step=0.02)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = H.inverse_fit(w, target.data_ptr(), ks.data_ptr(), b0_dev.data_ptr(), fs)
+    fit_s = time.perf_counter() - t0
     return {"workload": f"inverse erosion {n}x{n}, {nsteps} steps, per-cell Ks, checkpoints every {ckpt}",
             "forward_cell_steps_per_s": cs / (f / 1e3), "fwd_adjoint_cell_steps_per_s": cs / (a / 1e3),
-            "fwd_adjoint_over_forward_time": a / f, "ms_forward": f, "ms_fwd_adjoint": a}
+            "fwd_adjoint_over_forward_time": a / f, "ms_forward": f, "ms_fwd_adjoint": a,
+            "fit": {"iters": fit_iters, "ks_step": 0.01, "rock_step": 0.02, "ms_per_iter": fit_s * 1e3 / fit_iters,
+                    "loss_first": losses[0], "loss_last": losses[-1]}}
 
 
 def bench_large(H, torch, n=8192, fwd_steps=2000, adj_steps=512, nbatch=16, bn=1024, bsteps=256):

@@ -564,6 +564,38 @@ __global__ void k_sum_parts(const double* __restrict__ part, int nparts, double*
     *out = t;
 }
 
+// per-block max |g| (max is order-free, so the result does not depend on the split)
+__global__ void k_absmax_part(const float* __restrict__ g, size_t count, float* __restrict__ part) {
+    __shared__ float sh[256 / 32];
+    float m = 0.0f;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(g[i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t = fmaxf(t, sh[k]);
+        part[blockIdx.x] = t;
+    }
+}
+
+// x <- clamp(x - (step / max|g|) g, lo, hi): the largest change of any cell is `step`
+__global__ void k_descend(float* __restrict__ x, const float* __restrict__ g, size_t count,
+                          const float* __restrict__ part, int nparts, float step, float lo, float hi) {
+    __shared__ float a_sh;
+    if (threadIdx.x < 32) {
+        float m = 0.0f;
+        for (int k = threadIdx.x; k < nparts; k += 32) m = fmaxf(m, part[k]);
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) a_sh = step / fmaxf(m, 1e-30f);
+    }
+    __syncthreads();
+    const float a = a_sh;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        x[i] = fminf(fmaxf(x[i] - a * g[i], lo), hi);
+}
+
 dim3 grid_for(int n) { return dim3((n + BX - 1) / BX, (n + BY - 1) / BY); }
 
 }  // namespace
@@ -607,6 +639,13 @@ void launch_mse(const float* b, const float* target, size_t count, float* grad, 
                 double* out, cudaStream_t st) {
     k_mse_grad<<<nparts, 256, 0, st>>>(b, target, count, grad, part);
     k_sum_parts<<<1, 32, 0, st>>>(part, nparts, out);
+    count_launch(2);
+}
+
+void launch_descend(float* x, const float* g, size_t count, float step, float lo, float hi, float* part, int nparts,
+                    cudaStream_t st) {
+    k_absmax_part<<<nparts, 256, 0, st>>>(g, count, part);
+    k_descend<<<nparts * 4, 256, 0, st>>>(x, g, count, part, nparts, step, lo, hi);
     count_launch(2);
 }
 

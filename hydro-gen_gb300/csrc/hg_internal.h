@@ -285,6 +285,9 @@ void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const
 // loss = mean((b - target)^2) into *out (device), grad = dloss/db (optional).
 void launch_mse(const float* b, const float* target, size_t count, float* grad, double* part, int nparts,
                 double* out, cudaStream_t st);
+// x <- clamp(x - step * g / max|g|, lo, hi); part holds nparts floats
+void launch_descend(float* x, const float* g, size_t count, float step, float lo, float hi, float* part, int nparts,
+                    cudaStream_t st);
 
 // ---- init and reductions (hg_init.cu) ---------------------------------------------
 void launch_fbm_raw(float* out, int n, const hg_noise_settings& s, cudaStream_t st);

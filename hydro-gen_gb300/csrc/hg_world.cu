@@ -5,6 +5,7 @@
 // reduction scratch buffers.  hg_step sequences the passes the way
 // Erosion::dispatch_grid does (src/erosion.cpp:158-200), swapping buffer
 // pointers where the reference swaps Tex_pair read/write textures.
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1926,6 +1927,88 @@ int hg_mse(hg_world* w, const float* target, double* loss, float* dL_drock) {
     HG_CUDA(cudaMemcpyAsync(loss, res, sizeof(double), cudaMemcpyDeviceToHost, w->stream));
     HG_CUDA(cudaStreamSynchronize(w->stream));
     return HG_OK;
+}
+
+int hg_default_fit_settings(hg_fit_settings* out) {
+    if (!out) return fail(HG_ERR_INVALID, "null output");
+    out->nsteps = 256;
+    out->ckpt_every = 32;
+    out->iters = 8;
+    out->ks_step = 0.01f;
+    out->ks_min = 0.005f;
+    out->ks_max = 0.5f;
+    out->rock_step = 0.0f;
+    return HG_OK;
+}
+
+namespace {
+// device scratch of one fit: the loss adjoint, the two gradients and the losses
+struct FitScratch {
+    float* g = nullptr;
+    float* dks = nullptr;
+    float* db0 = nullptr;
+    double* losses = nullptr;
+    hg_tape* tape = nullptr;
+    ~FitScratch() {
+        cudaFree(g); cudaFree(dks); cudaFree(db0); cudaFree(losses);
+        if (tape) hg_tape_destroy(tape);
+    }
+};
+}  // namespace
+
+int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, const hg_fit_settings* s,
+                   double* losses) {
+    HG_CHECK_WORLD(w);
+    if (!s) return fail(HG_ERR_INVALID, "null fit settings");
+    if (!target || !rock0 || !losses) return fail(HG_ERR_INVALID, "null target, initial rock or losses");
+    if (s->iters < 1) return fail(HG_ERR_INVALID, "iters must be >= 1");
+    if (!(s->ks_step >= 0.0f) || !(s->rock_step >= 0.0f)) return fail(HG_ERR_INVALID, "steps must be >= 0");
+    if (s->ks_step > 0.0f && !ks) return fail(HG_ERR_INVALID, "fitting Ks needs a Ks buffer");
+    if (ks && !(s->ks_min >= 0.0f && s->ks_min <= s->ks_max))
+        return fail(HG_ERR_INVALID, "need 0 <= ks_min <= ks_max");
+    DeviceGuard g(w->device);
+    cudaStream_t st = w->stream;
+    const size_t c = cells(w), fb = c * sizeof(float);
+    FitScratch f;
+    int rc = hg_tape_create(w, s->nsteps, s->ckpt_every, &f.tape);
+    if (rc != HG_OK) return rc;
+    cudaError_t e = cudaMalloc((void**)&f.g, fb);
+    if (e == cudaSuccess && s->ks_step > 0.0f) e = cudaMalloc((void**)&f.dks, fb);
+    if (e == cudaSuccess && s->rock_step > 0.0f) e = cudaMalloc((void**)&f.db0, fb);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&f.losses, sizeof(double) * (size_t)s->iters);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(HG_ERR_OOM, "device allocation failed for the fit's gradients");
+    }
+    if (ks) {
+        HG_CUDA(cudaMemcpyAsync(w->ks, ks, fb, cudaMemcpyDeviceToDevice, st));
+        if (!w->ks_on) {
+            w->ks_on = true;
+            w->version += 1;
+        }
+    }
+    const uint64_t step0 = w->step;
+    const int parts = reduction_parts();
+    for (int it = 0; it < s->iters; ++it) {
+        rc = zero_state(w);
+        if (rc != HG_OK) return rc;
+        HG_CUDA(cudaMemcpyAsync(w->cur[S_ROCK], rock0, fb, cudaMemcpyDeviceToDevice, st));
+        w->step = step0;
+        w->dev_step_valid = false;
+        rc = hg_forward(f.tape);
+        if (rc != HG_OK) return rc;
+        launch_mse(w->cur[S_ROCK], target, c, f.g, w->red_d, parts, f.losses + it, st);
+        rc = hg_backward(f.tape, f.g, f.dks, f.db0);
+        if (rc != HG_OK) return rc;
+        // the Ks field is read by the next forward only, after both gradients exist
+        if (s->ks_step > 0.0f) launch_descend(w->ks, f.dks, c, s->ks_step, s->ks_min, s->ks_max, w->red_f, parts, st);
+        if (s->rock_step > 0.0f)
+            launch_descend(rock0, f.db0, c, s->rock_step, -FLT_MAX, FLT_MAX, w->red_f, parts, st);
+        HG_CUDA(cudaGetLastError());
+    }
+    if (ks) HG_CUDA(cudaMemcpyAsync(ks, w->ks, fb, cudaMemcpyDeviceToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(losses, f.losses, sizeof(double) * (size_t)s->iters, cudaMemcpyDeviceToHost, st));
+    return hg_sync(w);
 }
 
 namespace {

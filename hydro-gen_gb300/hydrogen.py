@@ -88,6 +88,12 @@ class NoiseSettings(ctypes.Structure):
                 ("out_max", ctypes.c_float)]
 
 
+class FitSettings(ctypes.Structure):
+    _fields_ = [("nsteps", ctypes.c_int32), ("ckpt_every", ctypes.c_int32), ("iters", ctypes.c_int32),
+                ("ks_step", ctypes.c_float), ("ks_min", ctypes.c_float), ("ks_max", ctypes.c_float),
+                ("rock_step", ctypes.c_float)]
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"{LIB_PATH} is missing: build it with hydro-gen_gb300/build.py (no CPU fallback)")
@@ -150,6 +156,8 @@ def _load():
         "hg_forward": (ctypes.c_int, [P]),
         "hg_backward": (ctypes.c_int, [P, P, P, P]),
         "hg_mse": (ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_double), P]),
+        "hg_default_fit_settings": (ctypes.c_int, [ctypes.POINTER(FitSettings)]),
+        "hg_inverse_fit": (ctypes.c_int, [P, P, P, P, ctypes.POINTER(FitSettings), ctypes.POINTER(ctypes.c_double)]),
         "hg_world_save": (ctypes.c_int, [P, ctypes.c_char_p]),
         "hg_world_load": (ctypes.c_int, [P, ctypes.c_char_p]),
     }
@@ -451,6 +459,27 @@ def mse(world, target_ptr, grad_ptr=None):
     loss = ctypes.c_double()
     check(lib.hg_mse(world.h, ctypes.c_void_p(target_ptr), ctypes.byref(loss), ctypes.c_void_p(grad_ptr or 0)))
     return loss.value
+
+
+def fit_settings(**kw):
+    """hg_fit_settings with the library defaults, fields overridden by keyword."""
+    s = FitSettings()
+    check(lib.hg_default_fit_settings(ctypes.byref(s)))
+    for k, v in kw.items():
+        if not hasattr(s, k):
+            raise AttributeError(f"hg_fit_settings has no field {k}")
+        setattr(s, k, v)
+    return s
+
+
+def inverse_fit(world, target_ptr, ks_ptr, rock0_ptr, settings=None):
+    """Native inverse-erosion descent (hg_inverse_fit) on device buffers;
+    returns the per-iteration losses."""
+    s = settings or fit_settings()
+    out = (ctypes.c_double * s.iters)()
+    check(lib.hg_inverse_fit(world.h, ctypes.c_void_p(target_ptr), ctypes.c_void_p(ks_ptr or 0),
+                             ctypes.c_void_p(rock0_ptr), ctypes.byref(s), out))
+    return list(out)
 
 
 class Batch:

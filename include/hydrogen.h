@@ -390,6 +390,36 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
  * pointers.  Synchronises. */
 int hg_mse(hg_world* w, const float* target, double* loss, float* dL_drock);
 
+/* Inverse erosion: descent on the per-cell Ks and the initial rock so that
+ * the rock after nsteps steps matches a target (the reference has no
+ * counterpart; its "Generate" button, src/rendering.cpp:193-202, only runs
+ * forward).  Every iteration resets the world to (rock0, no water, sediment,
+ * flux or velocity, the step counter of the call), records nsteps fused steps
+ * on a tape, takes the MSE loss against the target and its adjoint, and moves
+ * each fitted field by a normalised gradient step:
+ *   x <- clamp(x - step * g / max|g|, lo, hi)
+ * so that no cell changes by more than `step` per iteration. */
+typedef struct hg_fit_settings {
+    int32_t nsteps;      /* steps per forward */
+    int32_t ckpt_every;  /* checkpoint interval, HG_AUTO: about sqrt(nsteps) */
+    int32_t iters;       /* descent iterations (>= 1) */
+    float ks_step;       /* largest Ks change per iteration; 0 keeps Ks */
+    float ks_min, ks_max;  /* Ks stays in [ks_min, ks_max] */
+    float rock_step;     /* largest initial-rock change per iteration; 0 keeps rock0 */
+} hg_fit_settings;
+int hg_default_fit_settings(hg_fit_settings* out);
+/* target, ks and rock0 are device pointers to n*n floats.  ks (in/out, may be
+ * NULL when ks_step == 0: the world's Ks then stays) is the starting Ks field
+ * and receives the fitted one, which the world also keeps as its Ks field;
+ * rock0 (in/out) is the initial rock and receives the fitted one when
+ * rock_step > 0.  losses (host, iters doubles) receives the loss of each
+ * iteration, taken before its update.  The world is left at the end of the
+ * last iteration's forward.  The buffers are read and written on the
+ * world's stream: work that fills them on other streams must be complete.
+ * Same coverage as the tape (one layer, no smoothing).  Synchronises. */
+int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, const hg_fit_settings* s,
+                   double* losses);
+
 /* ---- checkpoint / resume ------------------------------------------------------------ */
 /* No counterpart in the reference (its state lives only in GL textures).
  * Writes the carried fields (rock, water, sediment, four fluxes, u, v; dirt

@@ -97,34 +97,90 @@ def test_tape_forward_is_the_fused_step(thermal):
         assert np.array_equal(a.download(f), b.download(f)), f
 
 
-def test_inverse_fit_reduces_loss():
-    """Fit per-cell Ks to a target made with a noise Ks field (config-4 form, small)."""
+def fit_problem(n, nsteps):
+    """Target: nsteps of the uniform-rain physics with a noise Ks field; the
+    fit starts from uniform Ks = 0.05 and the same initial rock."""
     torch = torch_dev()
-    n, nsteps = 64, 32
     truth = make_world(n, ks_seed=7)
     truth.step(nsteps, H.MODE_FUSED)
     target = torch.from_numpy(truth.download("rock")).cuda()
     w = make_world(n)
-    b0 = w.download("rock")
+    b0 = torch.from_numpy(w.download("rock")).cuda()
     ks = torch.full((n, n), 0.05, dtype=torch.float32, device="cuda")
+    return torch, w, target, b0, ks
+
+
+def descend(x, g, step, lo, hi):
+    """The normalised step of hg_inverse_fit in float32: x - (step / max|g|) g, clamped."""
+    a = np.float32(step) / np.maximum(np.abs(g).max(), np.float32(1e-30))
+    return np.minimum(np.maximum(x - np.float32(a) * g, np.float32(lo)), np.float32(hi))
+
+
+@pytest.mark.parametrize("rock_step", [0.0, 0.05])
+def test_inverse_fit_is_the_tape_loop(rock_step):
+    """hg_inverse_fit equals the same descent driven by hand through
+    hg_forward / hg_mse / hg_backward and a float32 update.  The sediment
+    adjoint scatters with float atomics, so the gradients' last bits follow
+    the atomics' order: the bar is a few ulps (rtol 1e-5), against a Ks
+    change of up to 1e-2 per iteration."""
+    n, nsteps, iters = 64, 24, 3
+    torch, w, target, b0, ks = fit_problem(n, nsteps)
+    s = H.fit_settings(nsteps=nsteps, ckpt_every=8, iters=iters, ks_step=0.01, rock_step=rock_step)
+    ks_fit, b_fit = ks.clone(), b0.clone()
+    torch.cuda.synchronize()  # the fit reads the buffers on the world's stream
+    losses = H.inverse_fit(w, target.data_ptr(), ks_fit.data_ptr(), b_fit.data_ptr(), s)
+    w_end = w.download("rock")
+
+    m = make_world(n)
+    ks_np, b_np = ks.cpu().numpy(), b0.cpu().numpy()
     g = torch.empty_like(ks)
     dks = torch.empty_like(ks)
-    losses = []
-    for it in range(6):
-        w.upload("rock", b0)
-        for f in ("water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b"):
-            w.upload(f, np.zeros((n, n), np.float32))
-        w.step_count = 0
-        w.upload_device("ks", ks.data_ptr())
-        tape = H.Tape(w, nsteps, 8)
+    db0 = torch.empty_like(ks)
+    tape = H.Tape(m, nsteps, 8)
+    ref = []
+    for _ in range(iters):
+        m.upload("rock", b_np)
+        for f in ("water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"):
+            m.upload(f, np.zeros((n, n), np.float32))
+        m.step_count = 0
+        m.upload("ks", ks_np)
         tape.forward()
-        losses.append(H.mse(w, target.data_ptr(), g.data_ptr()))
-        tape.backward(g.data_ptr(), dks.data_ptr(), None)
-        w.sync()
-        step = 1e-3 / max(float(dks.abs().max()), 1e-30)
-        ks = torch.clamp(ks - step * dks, 0.005, 0.5)
+        ref.append(H.mse(m, target.data_ptr(), g.data_ptr()))
+        tape.backward(g.data_ptr(), dks.data_ptr(), db0.data_ptr())
+        m.sync()
+        ks_np = descend(ks_np, dks.cpu().numpy(), 0.01, 0.005, 0.5)
+        if rock_step:
+            b_np = descend(b_np, db0.cpu().numpy(), rock_step, -np.finfo(np.float32).max, np.finfo(np.float32).max)
+    np.testing.assert_allclose(losses, ref, rtol=1e-5)
+    np.testing.assert_allclose(ks_fit.cpu().numpy(), ks_np, rtol=1e-5, atol=0)
+    np.testing.assert_allclose(b_fit.cpu().numpy(), b_np, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(w_end, m.download("rock"), rtol=1e-5, atol=1e-5)
+    assert np.array_equal(w.download("ks"), ks_fit.cpu().numpy())
+
+
+def test_inverse_fit_reduces_loss():
+    """Fit per-cell Ks and the initial rock to a target made with a noise Ks
+    field (the inverse-erosion workload's form, small)."""
+    n, nsteps = 64, 32
+    torch, w, target, b0, ks = fit_problem(n, nsteps)
+    s = H.fit_settings(nsteps=nsteps, ckpt_every=8, iters=8, ks_step=0.01, rock_step=0.02)
+    torch.cuda.synchronize()
+    losses = H.inverse_fit(w, target.data_ptr(), ks.data_ptr(), b0.data_ptr(), s)
     print("inverse fit losses", losses)
-    assert losses[-1] < losses[0]
+    assert losses[-1] < 0.5 * losses[0]
+    assert float(ks.min()) >= 0.005 and float(ks.max()) <= 0.5
+
+
+def test_inverse_fit_rejects_bad_arguments():
+    n = 64
+    torch, w, target, b0, ks = fit_problem(n, 4)
+    for kw in (dict(iters=0), dict(ks_step=-1.0), dict(ks_min=0.5, ks_max=0.1)):
+        s = H.fit_settings(nsteps=4, ckpt_every=2, **kw)
+        with pytest.raises(H.HydrogenError) as e:
+            H.inverse_fit(w, target.data_ptr(), ks.data_ptr(), b0.data_ptr(), s)
+        assert e.value.code == -1
+    with pytest.raises(H.HydrogenError):  # fitting Ks needs a Ks buffer
+        H.inverse_fit(w, target.data_ptr(), None, b0.data_ptr(), H.fit_settings(nsteps=4, iters=1))
 
 
 def test_adjoint_rejects_smoothing():
