@@ -218,6 +218,51 @@ def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fit_iters=8):
                     "loss_first": losses[0], "loss_last": losses[-1]}}
 
 
+def bench_adjoint_workload(H, torch, n=N_GRID, nsteps=100, reps=2):
+    """Forward + adjoint at the metric's workload (4096^2, Bernoulli rain,
+    talus slippage) with a per-cell Ks field: nsteps taped steps from the
+    initial heightmap, checkpoint interval chosen from free memory (the whole
+    tape fits here, so nothing is recomputed), MSE to a target, gradients for
+    Ks and the initial rock."""
+    w = H.World(n)
+    w.init_heightmap(H.noise(seed=0))
+    H.configure(w, "config2")
+    w.init_ks_field(H.noise(seed=7, octaves=3, frequency=1.0 / 256), 0.05, 0.5)
+    b0 = w.download("rock")
+    target = torch.from_numpy(b0).cuda().mul_(0.999)
+    g = torch.empty_like(target)
+    dks = torch.empty_like(target)
+    db0 = torch.empty_like(target)
+    tape = H.Tape(w, nsteps, H.HG_AUTO)
+    stream = torch.cuda.ExternalStream(w.stream)
+    res = []
+    for r in range(reps + 1):
+        w.upload("rock", b0)
+        for f in ("water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b"):
+            w.upload(f, np.zeros((n, n), np.float32))
+        w.step_count = 0
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        tape.forward()
+        e1.record(stream)
+        H.mse(w, target.data_ptr(), g.data_ptr())
+        tape.backward(g.data_ptr(), dks.data_ptr(), db0.data_ptr())
+        e2.record(stream)
+        e2.synchronize()
+        if r:
+            res.append((e0.elapsed_time(e1), e0.elapsed_time(e2)))
+    f = statistics.median(x[0] for x in res)
+    a = statistics.median(x[1] for x in res)
+    out = {"workload": f"{n}x{n} Bernoulli rain + talus slippage, per-cell Ks, {nsteps} steps",
+           "ckpt_every": tape.ckpt_every, "ms_forward": f, "ms_fwd_adjoint": a, "fwd_adjoint_over_forward_time": a / f,
+           "fwd_adjoint_cell_steps_per_s": n * n * nsteps / (a / 1e3),
+           "gradient_finite": bool(torch.isfinite(dks).all() and torch.isfinite(db0).all())}
+    tape.close()
+    w.close()
+    return out
+
+
 def bench_large(H, torch, n=8192, fwd_steps=2000, adj_steps=512, nbatch=16, bn=1024, bsteps=256):
     """The large workload: 8192^2, uniform-rain physics with talus slippage
     (tan 0.65, rate 0.3): 2000 forward steps; forward + adjoint over 512
@@ -754,6 +799,7 @@ def main():
     cpu = 0.0 if args.no_cpu_baseline else 6.0
     if not args.no_extras and single:
         line["fwd_adjoint"] = bench_adjoint(H, torch)
+        line["fwd_adjoint_4096"] = bench_adjoint_workload(H, torch)
         line["batch"] = bench_batch(H, torch)
         line["config1"] = bench_config1(H, torch, cpu=cpu > 0)
         line["large"] = bench_large(H, torch)

@@ -1,4 +1,4 @@
-// Reverse-mode adjoint of the grid step without thermal erosion.
+// Reverse-mode adjoint of the one-layer grid step (talus passes included).
 //
 // One reversed step j works on the step's input state X_j, the step's
 // forward intermediates kept by the segment recompute (velocity u, v and the
@@ -22,12 +22,17 @@
 //                   data dependent) and the back-trace velocity adjoint
 //   k_adj_sediment  the same scatter on its own, for a segment's last step
 //                   (its intermediates exist only after the recompute)
-//   k_adj_final     the gathered rock adjoint of the first state
+//   k_adj_final     the gathered rock adjoint of a state: of the first state
+//                   at the end, and with thermal erosion on, of each step's
+//                   output before k_adj_thermal
+//   k_adj_thermal   the talus passes reversed (rock adjoint after them ->
+//                   adjoint of the eroded rock, which k_adj_cell then takes)
 //
 // Subgradients: max(0, x) and min(1, q) pass the derivative of the taken
 // argument (ties take the constant side), clamps pass 0 when clamped,
 // dissolve/deposit/exhaustion use the taken branch, floor() is locally
-// constant.  The formulas follow the shaders cited in hg_device.cuh.  The
+// constant, and in water films below FILM_DEPTH the velocity and the flux
+// scale are locally constant.  The formulas follow the shaders cited in hg_device.cuh.  The
 // reversed arithmetic divides through correctly rounded reciprocals
 // (x * (1/y), within two ulps of x / y); the recomputed forward keeps IEEE
 // division, so its values and branches are the forward's own.
@@ -40,6 +45,14 @@ namespace {
 
 constexpr int BX = 32, BY = 8;
 __device__ __forceinline__ size_t at(int n, int x, int y) { return (size_t)y * n + x; }
+
+// Water films thinner than this (the depth below which the erosion ignores
+// the velocity, glsl/hydro_erosion.glsl:45-52) pass no adjoint through the
+// velocity (u = flux difference / depth) or the flux scale (K = depth /
+// outflow): both derivatives grow like 1/depth and overflow float in the
+// films that intermittent rain leaves (depths reach 1e-35), where they carry
+// no usable gradient anyway.
+constexpr float FILM_DEPTH = 5e-4f;
 
 // ---- sediment_transport reversed ------------------------------------------------
 // Cell (x, y) of a step whose output sediment adjoint is `a`: scatter to the
@@ -78,6 +91,9 @@ __global__ void k_adj_sediment(StepConsts c, AdjSlot sl, const float* __restrict
 
 // Gathered adjoint of a state at cell i: own terms plus the neighbours'
 // packets (L, R, T, B neighbours, fixed order).
+// ROCK false leaves ab alone (the caller has the rock adjoint from elsewhere)
+// and skips the loads only it needs
+template <bool ROCK = true>
 __device__ __forceinline__ void adj_view_at(const AdjView& A, int n, int x, int y, size_t i, float& ab, float& ad,
                                             float af[4]) {
     // w = rock + water: a neighbour's height difference toward this cell
@@ -87,12 +103,14 @@ __device__ __forceinline__ void adj_view_at(const AdjView& A, int n, int x, int 
     if (x < n - 1) nbw += A.pdh[0][i + 1];  // right neighbour's L
     if (y < n - 1) nbw += A.pdh[3][i + n];  // top neighbour's B
     if (y > 0) nbw += A.pdh[2][i - n];      // bottom neighbour's T
-    float nrm = 0.0f;  // terrain-normal terms of the neighbours
-    if (x > 0) nrm += A.pdx[i - 1];
-    if (x < n - 1) nrm -= A.pdx[i + 1];
-    if (y > 0) nrm += A.pdz[i - n];
-    if (y < n - 1) nrm -= A.pdz[i + n];
-    ab = (A.b[i] - nbw) + nrm;
+    if (ROCK) {
+        float nrm = 0.0f;  // terrain-normal terms of the neighbours
+        if (x > 0) nrm += A.pdx[i - 1];
+        if (x < n - 1) nrm -= A.pdx[i + 1];
+        if (y > 0) nrm += A.pdz[i - n];
+        if (y < n - 1) nrm -= A.pdz[i + n];
+        ab = (A.b[i] - nbw) + nrm;
+    }
     ad = A.d[i] - nbw;
 #pragma unroll
     for (int d = 0; d < 4; ++d) af[d] = A.f[d][i];
@@ -183,8 +201,12 @@ __device__ __forceinline__ void adj_tile(const AdjCellArgs& a, float* sm, uint64
     const int x = tx0 + ix, y = ty0 + iy;
     const size_t i = (size_t)y * n + x;
     float ab, ad, af[4];
-    adj_view_at(a.A, n, x, y, i, ab, ad, af);
-    if (a.gbe) ab = a.gbe[i];  // thermal on: the eroded rock's adjoint (k_adj_thermal)
+    if (a.gbe) {  // thermal on: the eroded rock's adjoint (k_adj_thermal)
+        ab = a.gbe[i];
+        adj_view_at<false>(a.A, n, x, y, i, ab, ad, af);
+    } else {
+        adj_view_at(a.A, n, x, y, i, ab, ad, af);
+    }
     const float as = a.dse[i];
     const float DUs = a.du[i], DVs = a.dv[i];
     const float Ks_i = c.ks_field ? c.ks_field[i] : c.Ks0;
@@ -299,7 +321,7 @@ __device__ __forceinline__ void adj_tile(const AdjCellArgs& a, float* sm, uint64
         // ---- flux reversed -------------------------------------------------
         const float DU = DUs + due, DV = DVs + dve;
         float gin[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gfown[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        if (vz > 0.0f) {
+        if (vz >= FILM_DEPTH) {  // thinner films: velocity locally constant
             const float rv = __frcp_rn(vz);
             float gu = DU * rv, gv = DV * rv;
             gin[0] += gu; gin[1] -= gu;
@@ -320,7 +342,7 @@ __device__ __forceinline__ void adj_tile(const AdjCellArgs& a, float* sm, uint64
         float gg[4];
 #pragma unroll
         for (int d = 0; d < 4; ++d) gg[d] = af[d] * fw.K + gsum_out;
-        if (fw.scaled) {
+        if (fw.scaled && d1 >= FILM_DEPTH) {  // thinner films: K locally constant
             const float rd = __frcp_rn(fw.den);
             gd1 += gK * rd;
             float gden = -gK * d1 * rd * rd;

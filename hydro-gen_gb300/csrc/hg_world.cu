@@ -1637,24 +1637,22 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     DeviceGuard g(w->device);
     const size_t c = cells(w);
     // Checkpoints (nsteps/K states) plus segment buffers (K states and
-    // slots each): K ~ sqrt(nsteps), two segment buffers when half the free
-    // memory holds them.  With HG_AUTO the interval nearest sqrt(nsteps)
-    // that fits is taken, two buffers first.
+    // slots each), within half the free memory.  The backward recomputes
+    // every segment but the last once, nsteps - K steps in all, so HG_AUTO
+    // takes the longest interval that fits (K = nsteps: nothing is
+    // recomputed); tape memory is smallest near K = sqrt(7 nsteps / 11),
+    // the fallback when nothing fits.  A second segment buffer, when it
+    // fits too, lets the recompute overlap the reverse sweep.
     size_t free_b = 0, total_b = 0;
     const size_t budget = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess ? free_b / 2 : (size_t)-1;
     int K = ckpt_every, nbuf = 1;
     if (K == HG_AUTO || K <= 0) {
-        const int K0 = std::min(nsteps, (int)std::ceil(std::sqrt((double)nsteps)));
         K = 0;
-        for (int nb = 2; nb >= 1 && K == 0; --nb)
-            for (int d = 0; d < nsteps && K == 0; ++d)
-                for (int cand : {K0 - d, K0 + d})
-                    if (cand >= 1 && cand <= nsteps && tape_bytes(c, nsteps, cand, nb) <= budget) {
-                        K = cand;
-                        nbuf = nb;
-                        break;
-                    }
-        if (K == 0) K = K0;  // nothing fits: let the allocation report it
+        for (int cand = nsteps; cand >= 1 && K == 0; --cand)
+            if (tape_bytes(c, nsteps, cand, 1) <= budget) K = cand;
+        if (K == 0)  // nothing fits: let the allocation report it
+            K = std::min(nsteps, std::max(1, (int)std::lround(std::sqrt(7.0 * nsteps / 11.0))));
+        nbuf = K < nsteps && tape_bytes(c, nsteps, K, 2) <= budget ? 2 : 1;
     } else {
         K = std::min(K, nsteps);
         nbuf = tape_bytes(c, nsteps, K, 2) <= budget ? 2 : 1;

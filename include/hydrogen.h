@@ -363,13 +363,14 @@ int hg_batch_launch_form(const hg_batch* b, int* per_world, double* ms_per_world
 int hg_world_totals(hg_world* w, double out[3]);
 
 /* ---- differentiation ------------------------------------------------------------------ */
-/* No counterpart in the reference.  Reverse-mode adjoint of the step without
- * thermal erosion (the talus passes must be off: Kspeed[0] == 0 or thermal
- * option 0), for fitting the per-cell rock solubility and the initial rock
- * heights.  A tape records nsteps steps of w with a checkpoint of the carried
- * fields every ckpt_every steps (HG_AUTO: about sqrt(nsteps), fewer if free
- * device memory is short); hg_backward recomputes each segment from its
- * checkpoint and runs the reverse kernels.  Subgradients at max/min/clamp
+/* No counterpart in the reference.  Reverse-mode adjoint of the one-layer
+ * step (rain, flux, erosion, sediment transport and, when on, the talus
+ * passes; not smoothing), for fitting the per-cell rock solubility and the
+ * initial rock heights.  A tape records nsteps steps of w with a checkpoint
+ * of the carried fields every ckpt_every steps (HG_AUTO: the longest
+ * interval whose tape fits in half the free device memory, up to nsteps,
+ * when nothing is recomputed); hg_backward recomputes each segment but the
+ * last from its checkpoint and runs the reverse kernels.  Subgradients at max/min/clamp
  * and at the dissolve/deposit branches: the taken branch's derivative.
  * The world's settings and per-cell Ks must not change between hg_forward
  * and hg_backward. */
@@ -401,7 +402,7 @@ int hg_mse(hg_world* w, const float* target, double* loss, float* dL_drock);
  * so that no cell changes by more than `step` per iteration. */
 typedef struct hg_fit_settings {
     int32_t nsteps;      /* steps per forward */
-    int32_t ckpt_every;  /* checkpoint interval, HG_AUTO: about sqrt(nsteps) */
+    int32_t ckpt_every;  /* checkpoint interval, HG_AUTO: the longest that fits */
     int32_t iters;       /* descent iterations (>= 1) */
     float ks_step;       /* largest Ks change per iteration; 0 keeps Ks */
     float ks_min, ks_max;  /* Ks stays in [ks_min, ks_max] */

@@ -13,7 +13,8 @@
 // Reverse mode with subgradients: max(0, x) and min(1, q) pass the
 // derivative of the taken argument (ties take the constant side), clamps
 // pass 0 when clamped, dissolve/deposit/exhaustion use the taken branch,
-// floor() is locally constant; the talus marks are locally constant, the
+// floor() is locally constant, velocity and flux scale are locally constant
+// in water films below kFilm; the talus marks are locally constant, the
 // largest drop H and the steepest slope pass their derivative to the
 // direction that attains them (the first in direction order).  Loss = mean((rock_final - target)^2);
 // gradients with respect to the per-cell rock solubility Ks and the initial
@@ -29,6 +30,12 @@ struct Params {
     double dt, G, EK, Kc, Kd0, Ke, amount, Kalpha, Kspeed;
     int period;
 };
+
+// Water films thinner than this (the float 5e-4 below which the erosion
+// ignores the velocity, glsl/hydro_erosion.glsl:45-52) pass no adjoint
+// through the velocity or the flux scale K (both derivatives grow like
+// 1/depth).
+const double kFilm = (double)5e-4f;
 
 // thermal directions L, R, T, B, LT, RT, LB, RB
 const int TOX[8] = {-1, 1, 0, 0, -1, 1, -1, 1};
@@ -379,7 +386,7 @@ struct Model {
                 double u = I.u[i], v = I.v[i];
                 // velocity
                 double gvz = dvz[i], gin[4] = {0, 0, 0, 0}, gfown[4] = {0, 0, 0, 0};
-                if (vz > 0) {
+                if (vz >= kFilm) {  // thinner films: velocity locally constant
                     gin[0] += du[i] / vz; gin[1] -= du[i] / vz;
                     gfown[0] -= du[i] / vz; gfown[1] += du[i] / vz;
                     gin[3] += dv[i] / vz; gin[2] -= dv[i] / vz;
@@ -395,7 +402,7 @@ struct Model {
                 for (int k = 0; k < 4; ++k) gK += A.f[k][i] * g[k];
                 double gg[4];
                 for (int k = 0; k < 4; ++k) gg[k] = A.f[k][i] * K + gsum_out;
-                if (q < 1.0) {  // K = q
+                if (q < 1.0 && d1 >= kFilm) {  // K = q; thinner films: K locally constant
                     gd1 += gK / den;
                     double gden = -gK * d1 / (den * den);
                     for (int k = 0; k < 4; ++k) gg[k] += gden * p.dt;
