@@ -318,22 +318,32 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
     const float4 u4 = __ldg(reinterpret_cast<const float4*>(td.u + gi0));
     const float4 v4 = __ldg(reinterpret_cast<const float4*>(td.v + gi0));
 
-    // sediment_transport: semi-Lagrangian gather of eroded sediment (any reach)
-    float sed[4];
+    // sediment_transport: semi-Lagrangian gather of eroded sediment (any
+    // reach).  The taps' loads stay in flight across the tile's TMA wait and
+    // the ring's outflows; the bilinear mix runs before the interior
+    // outflows, which need the registers (3.5 % of the step against mixing
+    // at once).
+    float bx[4], by[4], t00[4], t10[4], t01[4], t11[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        float px, py;
-        backtrace(c, x0 + j, y, at4(u4, j), at4(v4, j), px, py);
-        int ix = min(max((int)px, 0), n - 1), iy2 = min(max((int)py, 0), n - 1);
+        backtrace(c, x0 + j, y, at4(u4, j), at4(v4, j), bx[j], by[j]);
+        int ix = min(max((int)bx[j], 0), n - 1), iy2 = min(max((int)by[j], 0), n - 1);
         const float* se = td.s_ero + (size_t)iy2 * n + ix;
-        float s00 = __ldg(se);
-        float s10 = ix + 1 < n ? __ldg(se + 1) : 0.0f;
-        float s01 = iy2 + 1 < n ? __ldg(se + n) : 0.0f;
-        float s11 = (ix + 1 < n && iy2 + 1 < n) ? __ldg(se + n + 1) : 0.0f;
-        sed[j] = bilinear_mix(px, py, s00, s10, s01, s11);
+        t00[j] = __ldg(se);
+        t10[j] = ix + 1 < n ? __ldg(se + 1) : 0.0f;
+        t01[j] = iy2 + 1 < n ? __ldg(se + n) : 0.0f;
+        t11[j] = (ix + 1 < n && iy2 + 1 < n) ? __ldg(se + n + 1) : 0.0f;
     }
-    st4(td.out[S_SED] + gi0, make_float4(sed[0], sed[1], sed[2], sed[3]));
-    if (!c.thermal) return;
+    auto finish_sed = [&]() {
+        float sed[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sed[j] = bilinear_mix(bx[j], by[j], t00[j], t10[j], t01[j], t11[j]);
+        st4(td.out[S_SED] + gi0, make_float4(sed[0], sed[1], sed[2], sed[3]));
+    };
+    if (!c.thermal) {
+        finish_sed();
+        return;
+    }
 
     bool ok = __syncthreads_and(mbar_wait(bar, 0));
     if (!ok) {
@@ -341,6 +351,23 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
         mbar_wait(bar, 0);
         return;
     }
+    // ---- outflows of the ring of interior plus 1 ---------------------------
+    {
+        constexpr int RING = 2 * TW + 2 * (TH + 2);
+        for (int q = tid; q < RING; q += G::NTH) {
+            int rx, ry2;
+            if (q < TW) { rx = HX + q; ry2 = 1; }
+            else if (q < 2 * TW) { rx = HX + q - TW; ry2 = TH + 2; }
+            else if (q < 2 * TW + TH + 2) { rx = HX - 1; ry2 = 1 + q - 2 * TW; }
+            else { rx = HX + TW; ry2 = 1 + q - 2 * TW - (TH + 2); }
+            float o8[8];
+            outflows_scalar<EDGE>(c, be, rx, ry2, gx0 + rx, gy0 + ry2, o8);
+            const int ro = (ry2 - 1) * RW + rx;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) outf[d * O_C + ro] = o8[d];
+        }
+    }
+    finish_sed();
     // ---- outflows of the interior row groups (one per thread) --------------
     // The thread's own outflow sums (cell_thermal_apply's sum = 0 - own[0] -
     // ... - own[7]) stay in registers.
@@ -358,22 +385,6 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
         }
 #pragma unroll
         for (int d = 0; d < 8; ++d) st4(outf + d * O_C + oi, make_float4(o[d][0], o[d][1], o[d][2], o[d][3]));
-    }
-    // ---- outflows of the ring of interior plus 1 ---------------------------
-    {
-        constexpr int RING = 2 * TW + 2 * (TH + 2);
-        for (int q = tid; q < RING; q += G::NTH) {
-            int rx, ry2;
-            if (q < TW) { rx = HX + q; ry2 = 1; }
-            else if (q < 2 * TW) { rx = HX + q - TW; ry2 = TH + 2; }
-            else if (q < 2 * TW + TH + 2) { rx = HX - 1; ry2 = 1 + q - 2 * TW; }
-            else { rx = HX + TW; ry2 = 1 + q - 2 * TW - (TH + 2); }
-            float o8[8];
-            outflows_scalar<EDGE>(c, be, rx, ry2, gx0 + rx, gy0 + ry2, o8);
-            const int ro = (ry2 - 1) * RW + rx;
-#pragma unroll
-            for (int d = 0; d < 8; ++d) outf[d * O_C + ro] = o8[d];
-        }
     }
     __syncthreads();
     // ---- thermal_transport: own outflows out, neighbours' outflows in -------

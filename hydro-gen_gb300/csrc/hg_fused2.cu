@@ -216,29 +216,42 @@ __device__ __forceinline__ void transport_tile(const TransportArgs& a, float* be
     const int iy = tid / GPR, g = tid % GPR;
     const int x0 = tx0 + 4 * g, y = ty0 + iy;
     const size_t gi0 = (size_t)y * n + x0;
+    float bx[4], by[4], ta[4][4], tb[4][4];
     if (a.sediment) {
     const float4 u4 = __ldg(reinterpret_cast<const float4*>(a.u + gi0));
     const float4 v4 = __ldg(reinterpret_cast<const float4*>(a.v + gi0));
-    // sediment_transport, both channels: one back-trace, two gathers
-    float sa[4], sb[4];
+    // sediment_transport, both channels: one back-trace, two gathers.  The
+    // taps' loads stay in flight across the tile's TMA wait; the bilinear
+    // mixes follow it (later, the talus registers would spill).
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        float px, py;
-        backtrace(c, x0 + j, y, at4(u4, j), at4(v4, j), px, py);
-        const int ix = (int)px, iy2 = (int)py;  // px, py in [0, n - 1]
+        backtrace(c, x0 + j, y, at4(u4, j), at4(v4, j), bx[j], by[j]);
+        const int ix = (int)bx[j], iy2 = (int)by[j];  // in [0, n - 1]
         const bool hx = ix + 1 < n, hy = iy2 + 1 < n;
         const size_t o = (size_t)iy2 * n + ix;
         const float* p0 = a.s0 + o;
         const float* p1 = a.s1 + o;
-        sa[j] = bilinear_mix(px, py, __ldg(p0), hx ? __ldg(p0 + 1) : 0.0f, hy ? __ldg(p0 + n) : 0.0f,
-                             (hx && hy) ? __ldg(p0 + n + 1) : 0.0f);
-        sb[j] = bilinear_mix(px, py, __ldg(p1), hx ? __ldg(p1 + 1) : 0.0f, hy ? __ldg(p1 + n) : 0.0f,
-                             (hx && hy) ? __ldg(p1 + n + 1) : 0.0f);
+        ta[j][0] = __ldg(p0); ta[j][1] = hx ? __ldg(p0 + 1) : 0.0f;
+        ta[j][2] = hy ? __ldg(p0 + n) : 0.0f; ta[j][3] = (hx && hy) ? __ldg(p0 + n + 1) : 0.0f;
+        tb[j][0] = __ldg(p1); tb[j][1] = hx ? __ldg(p1 + 1) : 0.0f;
+        tb[j][2] = hy ? __ldg(p1 + n) : 0.0f; tb[j][3] = (hx && hy) ? __ldg(p1 + n + 1) : 0.0f;
     }
-    st4(a.s0_o + gi0, make_float4(sa[0], sa[1], sa[2], sa[3]));
-    st4(a.s1_o + gi0, make_float4(sb[0], sb[1], sb[2], sb[3]));
     }
-    if (!c.thermal) return;
+    auto finish_sed = [&]() {
+        if (!a.sediment) return;
+        float sa[4], sb[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            sa[j] = bilinear_mix(bx[j], by[j], ta[j][0], ta[j][1], ta[j][2], ta[j][3]);
+            sb[j] = bilinear_mix(bx[j], by[j], tb[j][0], tb[j][1], tb[j][2], tb[j][3]);
+        }
+        st4(a.s0_o + gi0, make_float4(sa[0], sa[1], sa[2], sa[3]));
+        st4(a.s1_o + gi0, make_float4(sb[0], sb[1], sb[2], sb[3]));
+    };
+    if (!c.thermal) {
+        finish_sed();
+        return;
+    }
 
     bool ok = __syncthreads_and(mbar_wait(bar, 0));
     if (!ok) {
@@ -246,6 +259,7 @@ __device__ __forceinline__ void transport_tile(const TransportArgs& a, float* be
         mbar_wait(bar, 0);
         return;
     }
+    finish_sed();
     // outflows of the interior (one row group per thread), own sums in registers
     const int rx0 = HX + 4 * g, ry = 2 + iy;
     const int oi = (ry - 1) * RW + rx0;
