@@ -51,7 +51,8 @@ def test_init_fbm_matches_oracle():
 
 
 @pytest.mark.parametrize("cfg,n,steps,p", [("config1", 64, 1, None), ("config1", 256, 100, None),
-                                           ("config2", 128, 60, 0.05), ("config2", 256, 100, None)])
+                                           ("config2", 128, 60, 0.05), ("config2", 256, 100, None),
+                                           ("config2", 200, 40, 0.05)])
 def test_plain_bitwise_vs_float_oracle(cfg, n, steps, p):
     w, ow, s, o = make_pair(n, cfg, p=p)
     for k in range(steps):
@@ -63,7 +64,8 @@ def test_plain_bitwise_vs_float_oracle(cfg, n, steps, p):
 
 
 @pytest.mark.parametrize("cfg,n,steps,p", [("config1", 256, 200, None), ("config2", 256, 200, 0.02),
-                                           ("config2", 512, 50, None), ("config1", 128, 30, None)])
+                                           ("config2", 512, 50, None), ("config1", 128, 30, None),
+                                           ("config2", 320, 60, 0.02)])
 def test_fused_bitwise_vs_plain(cfg, n, steps, p):
     a, _, _, _ = make_pair(n, cfg, p=p)
     b, _, _, _ = make_pair(n, cfg, p=p)
