@@ -22,11 +22,11 @@
 //                   data dependent) and the back-trace velocity adjoint
 //   k_adj_sediment  the same scatter on its own, for a segment's last step
 //                   (its intermediates exist only after the recompute)
-//   k_adj_final     the gathered rock adjoint of a state: of the first state
-//                   at the end, and with thermal erosion on, of each step's
-//                   output before k_adj_thermal
-//   k_adj_thermal   the talus passes reversed (rock adjoint after them ->
-//                   adjoint of the eroded rock, which k_adj_cell then takes)
+//   k_adj_final     the gathered rock adjoint of the first state
+//   k_adj_thermal   the talus passes reversed: gathers the output rock's
+//                   adjoint over its box from own terms and packets while
+//                   the eroded rock's box flies, and yields the adjoint of
+//                   the eroded rock, which k_adj_cell then takes
 //
 // Subgradients: max(0, x) and min(1, q) pass the derivative of the taken
 // argument (ties take the constant side), clamps pass 0 when clamped,
@@ -118,6 +118,21 @@ __device__ __forceinline__ void adj_view_at(const AdjView& A, int n, int x, int 
     if (x < n - 1) af[1] += A.pin[0][i + 1];  // right neighbour's inflow from me
     if (y < n - 1) af[2] += A.pin[3][i + n];  // top neighbour's inflow from me
     if (y > 0) af[3] += A.pin[2][i - n];      // bottom neighbour's inflow from me
+}
+
+// The gathered rock adjoint alone, with adj_view_at's operations and order.
+__device__ __forceinline__ float adj_rock_at(const AdjView& A, int n, int x, int y, size_t i) {
+    float nbw = 0.0f;
+    if (x > 0) nbw += A.pdh[1][i - 1];
+    if (x < n - 1) nbw += A.pdh[0][i + 1];
+    if (y < n - 1) nbw += A.pdh[3][i + n];
+    if (y > 0) nbw += A.pdh[2][i - n];
+    float nrm = 0.0f;
+    if (x > 0) nrm += A.pdx[i - 1];
+    if (x < n - 1) nrm -= A.pdx[i + 1];
+    if (y > 0) nrm += A.pdz[i - n];
+    if (y < n - 1) nrm -= A.pdz[i + n];
+    return (A.b[i] - nbw) + nrm;
 }
 
 // ---- k_adj_cell ------------------------------------------------------------------
@@ -419,9 +434,8 @@ __host__ __device__ constexpr int tt_oy(int k) { return (k == 2 || k == 4 || k =
 
 struct ThermalArgs {
     CUtensorMap map_b;  // eroded rock of the step (box TT_RW x TT_BH)
-    CUtensorMap map_a;  // gathered adjoint of the step's output rock (same box)
+    AdjView A;          // adjoint of the step's output (own terms + packets)
     StepConsts c;
-    const float* a;     // the same adjoint (global)
     float* g;           // out: adjoint of the eroded rock
 };
 
@@ -432,9 +446,19 @@ __device__ __forceinline__ void thermal_tile(const ThermalArgs& ta, float* bs, f
     const int n = c.n, tid = threadIdx.x;
     const int gx0 = tx0 - HX, gy0 = ty0 - 2;
     if (tid == 0) {
-        mbar_arrive_expect_tx(bar, 2 * TT_BOX * sizeof(float));
+        mbar_arrive_expect_tx(bar, TT_BOX * sizeof(float));
         tma_load_2d(bs, &ta.map_b, gx0, gy0, bar);
-        tma_load_2d(as, &ta.map_a, gx0, gy0, bar);
+    }
+    // while the eroded rock flies: the gathered adjoint A of the output rock
+    // over the region's columns 2 .. TT_RW - 3 (the tile, its ring and their
+    // neighbours), 0 outside the grid
+#pragma unroll 1
+    for (int q = tid; q < (TT_RW - 4) * TT_BH; q += TT_NTH) {
+        const int rx = 2 + q % (TT_RW - 4), ry = q / (TT_RW - 4);
+        const int x = gx0 + rx, y = gy0 + ry;
+        float v = 0.0f;
+        if (!EDGE || (x >= 0 && x < n && y >= 0 && y < n)) v = adj_rock_at(ta.A, n, x, y, (size_t)y * n + x);
+        as[ry * TT_RW + rx] = v;
     }
     bool ok = __syncthreads_and(mbar_wait(bar, 0));
     if (!ok) {
@@ -532,7 +556,7 @@ __device__ __forceinline__ void thermal_tile(const ThermalArgs& ta, float* bs, f
         const int ix = q % TW, iy = q / TW;
         const int x = tx0 + ix, y = ty0 + iy;
         const int rq = (iy + 1) * TT_CW + ix + 1;
-        float gsum = ta.a[(size_t)y * n + x] + gd[8 * TT_NC + rq];
+        float gsum = as[(iy + 2) * TT_RW + HX + ix] + gd[8 * TT_NC + rq];  // A(c), from the staged box
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int xx = x + tt_ox(k), yy = y + tt_oy(k);
@@ -645,13 +669,12 @@ void launch_adjoint_final(int n, const AdjView& A, float* out_b, cudaStream_t st
 
 int adjoint_thermal_box_rows() { return TT_BH; }
 
-void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const CUtensorMap& map_a,
-                            const float* a, float* g, int* err, cudaStream_t st) {
+void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const AdjView& A, float* g, int* err,
+                            cudaStream_t st) {
     ThermalArgs ta;
     ta.map_b = map_b;
-    ta.map_a = map_a;
+    ta.A = A;
     ta.c = c;
-    ta.a = a;
     ta.g = g;
     k_adj_thermal<<<(c.n / TW) * (c.n / TT_H), TT_NTH, 0, st>>>(ta, err);
     count_launch();

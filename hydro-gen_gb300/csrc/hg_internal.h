@@ -276,12 +276,12 @@ void launch_adjoint_sediment(const StepConsts& c, const AdjSlot& slot, const flo
 void launch_adjoint_cell(const AdjCellArgs& args, int* err, cudaStream_t st);
 // gathered rock adjoint of a state into out_b
 void launch_adjoint_final(int n, const AdjView& A, float* out_b, cudaStream_t st);
-// reverse of the talus passes: a (adjoint of the rock after them, gathered)
-// -> g (adjoint of the eroded rock); maps: boxes 72 x adjoint_thermal_box_rows()
-// of the eroded rock and of a
+// reverse of the talus passes: A (adjoint of the step's output, own terms and
+// packets; its rock part is gathered in the kernel) -> g (adjoint of the
+// eroded rock); map_b: boxes 72 x adjoint_thermal_box_rows() of the eroded rock
 int adjoint_thermal_box_rows();
-void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const CUtensorMap& map_a,
-                            const float* a, float* g, int* err, cudaStream_t st);
+void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const AdjView& A, float* g, int* err,
+                            cudaStream_t st);
 // loss = mean((b - target)^2) into *out (device), grad = dloss/db (optional).
 void launch_mse(const float* b, const float* target, size_t count, float* grad, double* part, int nparts,
                 double* out, cudaStream_t st);

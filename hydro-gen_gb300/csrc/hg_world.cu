@@ -1590,7 +1590,7 @@ struct hg_tape {
 namespace {
 constexpr int kStateFields = 7;
 constexpr int kSlotFields = 4;  // u, v, eroded sediment, eroded rock
-constexpr int kAuxFields = 6;   // 2 sediment-adjoint buffers, du, dv, gathered rock adjoint, eroded-rock adjoint
+constexpr int kAuxFields = 5;   // 2 sediment-adjoint buffers, du, dv, eroded-rock adjoint
 
 AdjFields fields_at(float* base, size_t c) {
     AdjFields f;
@@ -1811,8 +1811,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     float* dse[2] = {t->aux, t->aux + c};
     float* du = t->aux + 2 * c;
     float* dv = t->aux + 3 * c;
-    float* abf = t->aux + 4 * c;  // gathered adjoint of the rock after the talus passes
-    float* gbe = t->aux + 5 * c;  // adjoint of the eroded rock
+    float* gbe = t->aux + 4 * c;  // adjoint of the eroded rock
     // the final state's adjoint: rock only, no packets
     HG_CUDA(cudaMemsetAsync(t->adj, 0, 2 * sf * sizeof(float), st));
     HG_CUDA(cudaMemsetAsync(t->pk, 0, 2 * ADJ_PACKET_FIELDS * c * sizeof(float), st));
@@ -1879,13 +1878,11 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
             args.dse_prev = dse[(m + 1) & 1];
             args.gbe = nullptr;
             if (cst.thermal) {  // reverse the talus passes first: A's rock -> eroded rock's adjoint
-                launch_adjoint_final(w->n, view(cur), abf, st);
-                CUtensorMap mb, ma;
+                CUtensorMap mb;
                 const float* be = slot_of(j).u + 3 * c;
-                if (!t->tma.get(be, w->n, adjoint_thermal_box_rows(), &mb) ||
-                    !t->tma.get(abf, w->n, adjoint_thermal_box_rows(), &ma))
+                if (!t->tma.get(be, w->n, adjoint_thermal_box_rows(), &mb))
                     return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
-                launch_adjoint_thermal(cst, mb, ma, abf, gbe, w->err, st);
+                launch_adjoint_thermal(cst, mb, view(cur), gbe, w->err, st);
                 args.gbe = gbe;
             }
             args.scatter_prev = j > 0 ? 1 : 0;
