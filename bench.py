@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_GRID)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
-    ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint", "config1"],
+    ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint", "adjoint_thermal",
+                                        "config1"],
                     default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
@@ -693,6 +694,8 @@ def main():
             elif args.extra == "adjoint":  # --steps reversed steps, --warmup timed repetitions
                 out = bench_adjoint(H, torch, nsteps=args.steps, ckpt=min(32, args.steps),
                                     reps=max(1, args.warmup))
+            elif args.extra == "adjoint_thermal":  # --n grid, --steps taped steps, --warmup repetitions
+                out = bench_adjoint_workload(H, torch, n=args.n, nsteps=args.steps, reps=max(1, args.warmup))
             else:
                 out = bench_render(H, torch, frames=args.steps, warmup=args.warmup, cpu_budget_s=budget)
             print(json.dumps(out), flush=True)
