@@ -405,10 +405,7 @@ __global__ void k_adj_final(int n, AdjView A, float* __restrict__ out_b) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= n || y >= n) return;
-    size_t i = at(n, x, y);
-    float ab, ad, af[4];
-    adj_view_at(A, n, x, y, i, ab, ad, af);
-    out_b[i] = ab;
+    out_b[at(n, x, y)] = adj_rock_at(A, n, x, y, at(n, x, y));
 }
 
 // ---- k_adj_thermal ---------------------------------------------------------------

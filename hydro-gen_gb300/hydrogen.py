@@ -543,6 +543,25 @@ def config3_terrains(count=64, seed=0):
     return out
 
 
+def shard_by_area(sides, nranks):
+    """Owner rank of each terrain for a job of nranks ranks: greedy longest
+    processing time on cell counts (largest terrain first, ties by index,
+    each to the least-loaded rank, ties by rank).  Every rank computes the
+    same assignment from the manifest; terrains are independent, so the
+    ranks step their shares with no data exchange.  The largest load is
+    within one terrain of the mean."""
+    if nranks < 1:
+        raise ValueError("nranks must be >= 1")
+    area = [int(s) * int(s) for s in sides]
+    load = [0] * nranks
+    owner = [0] * len(area)
+    for i in sorted(range(len(area)), key=lambda k: (-area[k], k)):
+        r = min(range(nranks), key=lambda k: (load[k], k))
+        owner[i] = r
+        load[r] += area[i]
+    return owner
+
+
 def make_config3_world(t, terrain_id=0):
     w = World(t["n"])
     w.init_heightmap(noise(seed=t["seed"]))
