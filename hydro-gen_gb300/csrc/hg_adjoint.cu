@@ -418,10 +418,11 @@ __global__ void k_adj_final(int n, AdjView A, float* __restrict__ out_b) {
 //   their derivative to the direction that attains them (the first one in
 //   direction order); the marks themselves are locally constant.
 // dh_j = b(c) - b(neighbour j): +dL/ddh_j to the cell, - to the neighbour.
-// 64 x 8 tiles; the per-cell terms of the tile and its one-cell ring go
-// through shared memory, from TMA boxes of the eroded rock and A with a
-// two-cell halo.
-constexpr int TT_H = 8, TT_NTH = 256;
+// 64 x 16 tiles of 512 threads (the ring's share of the recomputed cells is
+// 16 % against 29 % for 64 x 8: 3 % less time); the per-cell terms of the
+// tile and its one-cell ring go through shared memory (54 KB, dynamic), from
+// a TMA box of the eroded rock and the gathered A, both with a two-cell halo.
+constexpr int TT_H = 16, TT_NTH = 512;
 constexpr int TT_RW = TW + 2 * HX, TT_BH = TT_H + 4, TT_BOX = TT_RW * TT_BH;
 constexpr int TT_BRC = ((TT_BOX + 31) / 32) * 32;
 constexpr int TT_CW = TW + 2, TT_CH = TT_H + 2, TT_NC = TT_CW * TT_CH;  // tile + ring
@@ -564,11 +565,14 @@ __device__ __forceinline__ void thermal_tile(const ThermalArgs& ta, float* bs, f
     }
 }
 
+constexpr size_t TT_SMEM = (2 * TT_BRC + 9 * TT_NC) * sizeof(float) + 8;
+
 __global__ void __launch_bounds__(TT_NTH) k_adj_thermal(const __grid_constant__ ThermalArgs ta, int* err) {
-    __shared__ __align__(128) float bs[TT_BRC];
-    __shared__ __align__(128) float as[TT_BRC];
-    __shared__ float gd[9 * TT_NC];
-    __shared__ __align__(8) uint64_t bar;
+    extern __shared__ __align__(128) float tdyn[];
+    float* bs = tdyn;
+    float* as = tdyn + TT_BRC;
+    float* gd = tdyn + 2 * TT_BRC;
+    uint64_t& bar = *reinterpret_cast<uint64_t*>(tdyn + 2 * TT_BRC + 9 * TT_NC);
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
     const int n = ta.c.n;
@@ -673,7 +677,8 @@ void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const
     ta.A = A;
     ta.c = c;
     ta.g = g;
-    k_adj_thermal<<<(c.n / TW) * (c.n / TT_H), TT_NTH, 0, st>>>(ta, err);
+    cudaFuncSetAttribute(k_adj_thermal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TT_SMEM);
+    k_adj_thermal<<<(c.n / TW) * (c.n / TT_H), TT_NTH, TT_SMEM, st>>>(ta, err);
     count_launch();
 }
 
