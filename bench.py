@@ -210,13 +210,14 @@ def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fit_iters=8):
     fs = H.fit_settings(nsteps=nsteps, ckpt_every=ckpt, iters=fit_iters, ks_step=0.01, rock_step=0.02)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    losses = H.inverse_fit(w, target.data_ptr(), ks.data_ptr(), b0_dev.data_ptr(), fs)
+    losses, norms = H.inverse_fit(w, target.data_ptr(), ks.data_ptr(), b0_dev.data_ptr(), fs, grad_norms=True)
     fit_s = time.perf_counter() - t0
     return {"workload": f"inverse erosion {n}x{n}, {nsteps} steps, per-cell Ks, checkpoints every {ckpt}",
             "forward_cell_steps_per_s": cs / (f / 1e3), "fwd_adjoint_cell_steps_per_s": cs / (a / 1e3),
             "fwd_adjoint_over_forward_time": a / f, "ms_forward": f, "ms_fwd_adjoint": a,
             "fit": {"iters": fit_iters, "ks_step": 0.01, "rock_step": 0.02, "ms_per_iter": fit_s * 1e3 / fit_iters,
-                    "loss_first": losses[0], "loss_last": losses[-1]}}
+                    "loss_first": losses[0], "loss_last": losses[-1], "grad_norm_first": norms[0],
+                    "grad_norm_last": norms[-1]}}
 
 
 def bench_adjoint_workload(H, torch, n=N_GRID, nsteps=100, reps=2):

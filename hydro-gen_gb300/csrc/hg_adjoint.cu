@@ -611,6 +611,30 @@ __global__ void k_sum_parts(const double* __restrict__ part, int nparts, double*
     *out = t;
 }
 
+// per-block sums of g^2 in FP64 (the gradient norm's accumulation)
+__global__ void k_sumsq_part(const float* __restrict__ g, size_t count, double* __restrict__ part) {
+    __shared__ double sh[256 / 32];
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        acc += (double)g[i] * (double)g[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
+        part[blockIdx.x] = t;
+    }
+}
+
+// *out += sum of the partials (fixed order)
+__global__ void k_add_parts(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    double t = 0.0;
+    for (int k = 0; k < nparts; ++k) t += part[k];
+    *out += t;
+}
+
 // per-block max |g| (max is order-free, so the result does not depend on the split)
 __global__ void k_absmax_part(const float* __restrict__ g, size_t count, float* __restrict__ part) {
     __shared__ float sh[256 / 32];
@@ -686,6 +710,12 @@ void launch_mse(const float* b, const float* target, size_t count, float* grad, 
                 double* out, cudaStream_t st) {
     k_mse_grad<<<nparts, 256, 0, st>>>(b, target, count, grad, part);
     k_sum_parts<<<1, 32, 0, st>>>(part, nparts, out);
+    count_launch(2);
+}
+
+void launch_add_sumsq(const float* g, size_t count, double* part, int nparts, double* out, cudaStream_t st) {
+    k_sumsq_part<<<nparts, 256, 0, st>>>(g, count, part);
+    k_add_parts<<<1, 32, 0, st>>>(part, nparts, out);
     count_launch(2);
 }
 

@@ -1952,7 +1952,7 @@ struct FitScratch {
 }  // namespace
 
 int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, const hg_fit_settings* s,
-                   double* losses) {
+                   double* losses, double* grad_norms) {
     HG_CHECK_WORLD(w);
     if (!s) return fail(HG_ERR_INVALID, "null fit settings");
     if (!target || !rock0 || !losses) return fail(HG_ERR_INVALID, "null target, initial rock or losses");
@@ -1970,7 +1970,7 @@ int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, co
     cudaError_t e = cudaMalloc((void**)&f.g, fb);
     if (e == cudaSuccess && s->ks_step > 0.0f) e = cudaMalloc((void**)&f.dks, fb);
     if (e == cudaSuccess && s->rock_step > 0.0f) e = cudaMalloc((void**)&f.db0, fb);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&f.losses, sizeof(double) * (size_t)s->iters);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&f.losses, sizeof(double) * 2 * (size_t)s->iters);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(HG_ERR_OOM, "device allocation failed for the fit's gradients");
@@ -1995,6 +1995,12 @@ int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, co
         launch_mse(w->cur[S_ROCK], target, c, f.g, w->red_d, parts, f.losses + it, st);
         rc = hg_backward(f.tape, f.g, f.dks, f.db0);
         if (rc != HG_OK) return rc;
+        if (grad_norms) {  // squared norm over the fitted fields, FP64
+            double* sq = f.losses + s->iters + it;
+            HG_CUDA(cudaMemsetAsync(sq, 0, sizeof(double), st));
+            if (f.dks) launch_add_sumsq(f.dks, c, w->red_d, parts, sq, st);
+            if (f.db0) launch_add_sumsq(f.db0, c, w->red_d, parts, sq, st);
+        }
         // the Ks field is read by the next forward only, after both gradients exist
         if (s->ks_step > 0.0f) launch_descend(w->ks, f.dks, c, s->ks_step, s->ks_min, s->ks_max, w->red_f, parts, st);
         if (s->rock_step > 0.0f)
@@ -2003,7 +2009,13 @@ int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, co
     }
     if (ks) HG_CUDA(cudaMemcpyAsync(ks, w->ks, fb, cudaMemcpyDeviceToDevice, st));
     HG_CUDA(cudaMemcpyAsync(losses, f.losses, sizeof(double) * (size_t)s->iters, cudaMemcpyDeviceToHost, st));
-    return hg_sync(w);
+    if (grad_norms)
+        HG_CUDA(cudaMemcpyAsync(grad_norms, f.losses + s->iters, sizeof(double) * (size_t)s->iters,
+                                cudaMemcpyDeviceToHost, st));
+    const int src = hg_sync(w);
+    if (src == HG_OK && grad_norms)
+        for (int it = 0; it < s->iters; ++it) grad_norms[it] = std::sqrt(grad_norms[it]);
+    return src;
 }
 
 namespace {

@@ -157,7 +157,8 @@ def _load():
         "hg_backward": (ctypes.c_int, [P, P, P, P]),
         "hg_mse": (ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_double), P]),
         "hg_default_fit_settings": (ctypes.c_int, [ctypes.POINTER(FitSettings)]),
-        "hg_inverse_fit": (ctypes.c_int, [P, P, P, P, ctypes.POINTER(FitSettings), ctypes.POINTER(ctypes.c_double)]),
+        "hg_inverse_fit": (ctypes.c_int, [P, P, P, P, ctypes.POINTER(FitSettings), ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
         "hg_world_save": (ctypes.c_int, [P, ctypes.c_char_p]),
         "hg_world_load": (ctypes.c_int, [P, ctypes.c_char_p]),
     }
@@ -472,14 +473,16 @@ def fit_settings(**kw):
     return s
 
 
-def inverse_fit(world, target_ptr, ks_ptr, rock0_ptr, settings=None):
+def inverse_fit(world, target_ptr, ks_ptr, rock0_ptr, settings=None, grad_norms=False):
     """Native inverse-erosion descent (hg_inverse_fit) on device buffers;
-    returns the per-iteration losses."""
+    returns the per-iteration losses (and, with grad_norms, the FP64 norms
+    of each iteration's gradient)."""
     s = settings or fit_settings()
     out = (ctypes.c_double * s.iters)()
+    gn = (ctypes.c_double * s.iters)() if grad_norms else None
     check(lib.hg_inverse_fit(world.h, ctypes.c_void_p(target_ptr), ctypes.c_void_p(ks_ptr or 0),
-                             ctypes.c_void_p(rock0_ptr), ctypes.byref(s), out))
-    return list(out)
+                             ctypes.c_void_p(rock0_ptr), ctypes.byref(s), out, gn))
+    return (list(out), list(gn)) if grad_norms else list(out)
 
 
 class Batch:

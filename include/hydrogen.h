@@ -414,12 +414,15 @@ int hg_default_fit_settings(hg_fit_settings* out);
  * and receives the fitted one, which the world also keeps as its Ks field;
  * rock0 (in/out) is the initial rock and receives the fitted one when
  * rock_step > 0.  losses (host, iters doubles) receives the loss of each
- * iteration, taken before its update.  The world is left at the end of the
+ * iteration, taken before its update; grad_norms (host, iters doubles, may
+ * be NULL) the L2 norm of that iteration's gradient over the fitted fields
+ * (Ks and/or the initial rock), accumulated in FP64 on the device.  The
+ * world is left at the end of the
  * last iteration's forward.  The buffers are read and written on the
  * world's stream: work that fills them on other streams must be complete.
  * Same coverage as the tape (one layer, no smoothing).  Synchronises. */
 int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, const hg_fit_settings* s,
-                   double* losses);
+                   double* losses, double* grad_norms);
 
 /* ---- checkpoint / resume ------------------------------------------------------------ */
 /* No counterpart in the reference (its state lives only in GL textures).

@@ -147,7 +147,7 @@ def test_inverse_fit_is_the_tape_loop(rock_step):
     s = H.fit_settings(nsteps=nsteps, ckpt_every=8, iters=iters, ks_step=0.01, rock_step=rock_step)
     ks_fit, b_fit = ks.clone(), b0.clone()
     torch.cuda.synchronize()  # the fit reads the buffers on the world's stream
-    losses = H.inverse_fit(w, target.data_ptr(), ks_fit.data_ptr(), b_fit.data_ptr(), s)
+    losses, norms = H.inverse_fit(w, target.data_ptr(), ks_fit.data_ptr(), b_fit.data_ptr(), s, grad_norms=True)
     w_end = w.download("rock")
 
     m = make_world(n)
@@ -156,7 +156,7 @@ def test_inverse_fit_is_the_tape_loop(rock_step):
     dks = torch.empty_like(ks)
     db0 = torch.empty_like(ks)
     tape = H.Tape(m, nsteps, 8)
-    ref = []
+    ref, ref_norms = [], []
     for _ in range(iters):
         m.upload("rock", b_np)
         for f in ("water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"):
@@ -167,10 +167,15 @@ def test_inverse_fit_is_the_tape_loop(rock_step):
         ref.append(H.mse(m, target.data_ptr(), g.data_ptr()))
         tape.backward(g.data_ptr(), dks.data_ptr(), db0.data_ptr())
         m.sync()
+        sq = np.sum(dks.cpu().numpy().astype(np.float64) ** 2)
+        if rock_step:
+            sq += np.sum(db0.cpu().numpy().astype(np.float64) ** 2)
+        ref_norms.append(np.sqrt(sq))
         ks_np = descend(ks_np, dks.cpu().numpy(), 0.01, 0.005, 0.5)
         if rock_step:
             b_np = descend(b_np, db0.cpu().numpy(), rock_step, -np.finfo(np.float32).max, np.finfo(np.float32).max)
     np.testing.assert_allclose(losses, ref, rtol=1e-5)
+    np.testing.assert_allclose(norms, ref_norms, rtol=1e-4)  # FP64 on the device, FP64 here
     np.testing.assert_allclose(ks_fit.cpu().numpy(), ks_np, rtol=1e-5, atol=0)
     np.testing.assert_allclose(b_fit.cpu().numpy(), b_np, rtol=1e-5, atol=1e-5)
     np.testing.assert_allclose(w_end, m.download("rock"), rtol=1e-5, atol=1e-5)
