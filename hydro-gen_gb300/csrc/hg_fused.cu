@@ -108,7 +108,6 @@ __device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorM
     using G = Geo<TH>;
     constexpr int NTH = G::NTH, H_RC = G::H_RC, H_RH = G::H_RH;
     const StepConsts& c = td.c;
-    const RainStep r = rain_for(td.rain, *td.step + 1ull);
     const int n = c.n;
     const int tid = threadIdx.x;
     const int gx0 = tx0 - HX, gy0 = ty0 - 1;
@@ -117,6 +116,8 @@ __device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorM
 #pragma unroll
         for (int f = 0; f < H_N; ++f) tma_load_2d(sm + f * H_RC, &maps[f], gx0, gy0, bar);
     }
+    // the step counter's load overlaps the tiles' copies
+    const RainStep r = rain_for(td.rain, *td.step + 1ull);
     // rain words of the region's row groups, drawn while the tiles load
     constexpr int RG = (RW / 4) * H_RH;
     constexpr int RGK = (RG + NTH - 1) / NTH;
