@@ -7,6 +7,7 @@
 // two ulps) and a third next to the midpoint between two floats, the cases
 // where a quotient rounds wrongly first.
 #include "hg_internal.h"
+#include "hg_tma.cuh"
 
 namespace hg {
 namespace {
@@ -54,8 +55,48 @@ __global__ void k_selftest_division(uint32_t seed_lo, uint32_t seed_hi, unsigned
     if (local) atomicAdd(bad, local);
 }
 
+// The kernels' bounded wait on a barrier phase that never completes: one
+// arrival is expected and none comes, and no copy is in flight.  Thread 0
+// records whether the wait gave up and how long `polls` polls took.
+__global__ void k_selftest_wait(uint32_t polls, int* timed_out, unsigned long long* ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    unsigned long long t0, t1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    const bool ok = __syncthreads_and(mbar_wait_n(&bar, 0, polls));
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    if (threadIdx.x == 0) {
+        *timed_out = ok ? 0 : 1;
+        *ns = t1 - t0;
+    }
+}
+
 }  // namespace
 }  // namespace hg
+
+extern "C" int hg_selftest_bounded_wait(uint32_t polls, int* timed_out, double* ns_per_poll) {
+    using namespace hg;
+    if (!timed_out || !ns_per_poll) return hg_report_error(HG_ERR_INVALID, "null output pointer");
+    if (polls < 1 || polls > kMaxPolls) return hg_report_error(HG_ERR_INVALID, "polls must be in [1, 2^18]");
+    int* d = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d, 16);
+    if (e == cudaSuccess) e = cudaMemset(d, 0, 16);
+    if (e == cudaSuccess) {
+        k_selftest_wait<<<1, 32>>>(polls, d, reinterpret_cast<unsigned long long*>(d + 2));
+        count_launch();
+        e = cudaGetLastError();
+    }
+    int flag = 0;
+    unsigned long long ns = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, d, sizeof(flag), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&ns, d + 2, sizeof(ns), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return hg_report_error(HG_ERR_CUDA, cudaGetErrorString(e));
+    *timed_out = flag;
+    *ns_per_poll = (double)ns / polls;
+    return HG_OK;
+}
 
 extern "C" int hg_selftest_division(uint64_t seed, uint64_t count, uint64_t* mismatches) {
     using namespace hg;

@@ -7,7 +7,10 @@
 
 namespace hg {
 
-constexpr uint32_t kMaxPolls = 1u << 22;
+// A poll of a phase that has not completed returns after about 3.8 us on a
+// GB300 (measured by hg_selftest_bounded_wait), so a lost tile is given up
+// after about 1 s; a tile's copy completes within microseconds.
+constexpr uint32_t kMaxPolls = 1u << 18;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -24,10 +27,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  : "memory");
 }
 
-// true once the barrier's phase `parity` has completed; false after kMaxPolls polls
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// true once the barrier's phase `parity` has completed; false after `polls` polls
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, uint32_t polls) {
     const uint32_t a = smem_addr(bar);
-    for (uint32_t i = 0; i < kMaxPolls; ++i) {
+    for (uint32_t i = 0; i < polls; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -40,6 +43,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     }
     return false;
 }
+
+// the kernels' wait: true once phase `parity` has completed; false after kMaxPolls polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) { return mbar_wait_n(bar, parity, kMaxPolls); }
 
 // 2-D tiled load of the box at element coordinates (x, y) into shared memory;
 // completion is counted on `bar` in bytes.  x * 4 bytes must be a multiple of 16.

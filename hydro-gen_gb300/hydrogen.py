@@ -147,6 +147,8 @@ def _load():
         "hg_particles_count": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int)]),
         "hg_particles_get": (ctypes.c_int, [P, P, P, P]),
         "hg_selftest_division": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
+        "hg_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_uint32, ctypes.POINTER(ctypes.c_int),
+                                                    ctypes.POINTER(ctypes.c_double)]),
         "hg_batch_launch_form": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
         "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_double)]),

@@ -466,6 +466,13 @@ int hg_field_totals_noalloc(const float* const* fields, int nfields, size_t coun
  * (Markstein's correction) and counts results that differ in any bit from
  * IEEE division; 0 is the only passing answer.  Synchronises. */
 int hg_selftest_division(uint64_t seed, uint64_t count, uint64_t* mismatches);
+/* The kernels' bounded barrier wait (a TMA tile that never arrives) run on a
+ * barrier phase that nothing completes, with no copy in flight: `polls`
+ * polls (1 .. 2^18, the kernels' limit), after which the wait gives up.
+ * timed_out receives 1 when it did, ns_per_poll the measured time per poll,
+ * so 2^18 * ns_per_poll bounds a kernel's wait for a lost tile (about 1 s).  The device
+ * stays usable afterwards.  Synchronises. */
+int hg_selftest_bounded_wait(uint32_t polls, int* timed_out, double* ns_per_poll);
 
 #ifdef __cplusplus
 }

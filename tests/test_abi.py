@@ -65,6 +65,13 @@ def test_error_paths_without_a_device(hg):
     assert hg.lib.hg_world_create(64, 3, ctypes.byref(h)) == -5  # layers 1 (rock) or 2 (rock + dirt)
     assert hg.lib.hg_step(None, 1, 0) == -1
     assert hg.lib.hg_world_destroy(None) == 0
+    flag, ns = ctypes.c_int(), ctypes.c_double()
+    assert hg.lib.hg_selftest_bounded_wait(0, ctypes.byref(flag), ctypes.byref(ns)) == -1
+    assert hg.lib.hg_selftest_bounded_wait((1 << 18) + 1, ctypes.byref(flag), ctypes.byref(ns)) == -1
+    fs = hg.FitSettings()
+    assert hg.lib.hg_default_fit_settings(ctypes.byref(fs)) == 0
+    assert (fs.nsteps, fs.ckpt_every, fs.iters) == (256, 32, 8)
+    assert hg.lib.hg_inverse_fit(None, None, None, None, ctypes.byref(fs), None, None) == -1
 
 
 def test_header_cites_reference():
