@@ -165,6 +165,20 @@ void launch_ks_from_fbm(float* x, size_t count, float base, float k_over_amp, cu
     count_launch();
 }
 
+// NaN and infinite values of x (exponent bits all ones), added to *out
+__global__ void k_nonfinite(const float* __restrict__ x, size_t count, unsigned long long* __restrict__ out) {
+    unsigned long long k = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
+        k += (__float_as_uint(x[i]) & 0x7f800000u) == 0x7f800000u ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+    if ((threadIdx.x & 31) == 0 && k) atomicAdd(out, k);
+}
+
+void launch_count_nonfinite(const float* x, size_t count, unsigned long long* out, cudaStream_t st) {
+    k_nonfinite<<<RED_PARTS * 4, 256, 0, st>>>(x, count, out);
+    count_launch();
+}
+
 void launch_sum_f64(const PtrList8& fields, int nfields, size_t count, double* partial, int nparts,
                     double* out, cudaStream_t st) {
     k_sum_part<<<nparts, RED_THREADS, 0, st>>>(fields, nfields, count, partial);

@@ -285,6 +285,8 @@ void launch_adjoint_thermal(const StepConsts& c, const CUtensorMap& map_b, const
 // loss = mean((b - target)^2) into *out (device), grad = dloss/db (optional).
 void launch_mse(const float* b, const float* target, size_t count, float* grad, double* part, int nparts,
                 double* out, cudaStream_t st);
+// *out += the count of NaN and infinite values of x
+void launch_count_nonfinite(const float* x, size_t count, unsigned long long* out, cudaStream_t st);
 // *out += sum of g^2 in FP64 (fixed order); part holds nparts doubles
 void launch_add_sumsq(const float* g, size_t count, double* part, int nparts, double* out, cudaStream_t st);
 // x <- clamp(x - step * g / max|g|, lo, hi); part holds nparts floats

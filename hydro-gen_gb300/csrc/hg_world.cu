@@ -16,6 +16,8 @@
 
 #include <limits>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "hg_internal.h"
 
 namespace hg {
@@ -169,10 +171,26 @@ namespace {
 
 thread_local std::string t_err;
 
+// the host log hook (hg_set_log_callback); set rarely, read on every report
+std::atomic<hg_log_fn> g_log_fn{nullptr};
+std::atomic<void*> g_log_user{nullptr};
+
+void log_msg(int level, const std::string& msg) {
+    if (hg_log_fn fn = g_log_fn.load(std::memory_order_acquire)) fn(level, msg.c_str(), g_log_user.load());
+}
+
 int fail(int code, const std::string& msg) {
     t_err = msg;
+    log_msg(HG_LOG_ERROR, msg);
     return code;
 }
+
+// NVTX range over an entry point (visible in Nsight timelines; header-only
+// NVTX3, a no-op when no tool is attached)
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
 
 int cuda_fail(cudaError_t e, const char* what) {
     cudaGetLastError();  // clear a sticky launch error so later calls report their own
@@ -601,6 +619,11 @@ int fused_run(Plan** plans, const std::vector<hg_world*>& worlds, Tuning& tune, 
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         nsteps -= 8;
+        char m[160];
+        std::snprintf(m, sizeof m, "autotuner: %zu world(s), tile 64x%d, graph %s (ms/step: %.4f %.4f %.4f %.4f)",
+                      worlds.size(), tune.th, tune.graph ? "on" : "off", tune.ms[0], tune.ms[1], tune.ms[2],
+                      tune.ms[3]);
+        log_msg(HG_LOG_INFO, m);
     }
     int th = req_th != HG_AUTO ? req_th : (tune.th ? tune.th : 16);
     int graph = req_graph != HG_AUTO ? req_graph : (tune.th ? tune.graph : 1);
@@ -636,6 +659,12 @@ extern "C" {
 
 const char* hg_version(void) { return "hydrogen-gb300 0.1 (sm_103a)"; }
 const char* hg_last_error(void) { return t_err.c_str(); }
+
+int hg_set_log_callback(hg_log_fn fn, void* user) {
+    g_log_user.store(user, std::memory_order_relaxed);
+    g_log_fn.store(fn, std::memory_order_release);
+    return HG_OK;
+}
 uint64_t hg_launch_count(void) { return g_launches.load(); }
 
 int hg_default_erosion_settings(hg_erosion_settings* out) {
@@ -910,6 +939,7 @@ int hg_set_map_settings(hg_world* w, const hg_map_settings* s) {
 }
 
 int hg_init_reference_heightmap(hg_world* w, const hg_map_settings* s) {
+    Range nv_range("hg_init_reference_heightmap");
     HG_CHECK_WORLD(w);
     int rc = check_map_settings(s);
     if (rc != HG_OK) return rc;
@@ -971,6 +1001,7 @@ int hg_camera_look_at(hg_camera* out, const float pos[3], const float dir[3], co
 }
 
 int hg_render_device(hg_world* w, const hg_camera* cam, int width, int height, uint8_t* rgba_dev, float* rgb_dev) {
+    Range nv_range("hg_render_device");
     HG_CHECK_WORLD(w);
     if (!cam || !rgba_dev) return fail(HG_ERR_INVALID, "null argument");
     if (width < 1 || height < 1 || (size_t)width * height > (size_t)1 << 28)
@@ -989,6 +1020,7 @@ int hg_render_device(hg_world* w, const hg_camera* cam, int width, int height, u
 }
 
 int hg_render(hg_world* w, const hg_camera* cam, int width, int height, uint8_t* rgba, float* rgb) {
+    Range nv_range("hg_render");
     HG_CHECK_WORLD(w);
     if (!cam || !rgba) return fail(HG_ERR_INVALID, "null argument");
     if (width < 1 || height < 1 || (size_t)width * height > (size_t)1 << 28)
@@ -1108,6 +1140,7 @@ int hg_particles_count(const hg_world* w, int* count) {
 }
 
 int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
+    Range nv_range("hg_init_heightmap");
     HG_CHECK_WORLD(w);
     if (!s) return fail(HG_ERR_INVALID, "null noise settings");
     if (s->octaves < 1 || s->octaves > 32) return fail(HG_ERR_INVALID, "octaves must be in [1, 32]");
@@ -1121,6 +1154,40 @@ int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
     HG_CUDA(cudaGetLastError());
     w->step = 0;
     w->dev_step_valid = false;
+    return HG_OK;
+}
+
+int hg_world_count_nonfinite(hg_world* w, uint64_t* count) {
+    HG_CHECK_WORLD(w);
+    if (!count) return fail(HG_ERR_INVALID, "null output");
+    DeviceGuard g(w->device);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(w->red_d);  // 8 bytes of reduction scratch
+    HG_CUDA(cudaMemsetAsync(d, 0, sizeof(*d), w->stream));
+    const size_t c = cells(w);
+    for (int f = 0; f < S_COUNT; ++f) launch_count_nonfinite(w->cur[f], c, d, w->stream);
+    launch_count_nonfinite(w->u, c, d, w->stream);
+    launch_count_nonfinite(w->v, c, d, w->stream);
+    if (w->layers == 2) {
+        launch_count_nonfinite(w->dirt[0], c, d, w->stream);
+        launch_count_nonfinite(w->sdirt[0], c, d, w->stream);
+    }
+    HG_CUDA(cudaGetLastError());
+    unsigned long long h = 0;
+    HG_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, w->stream));
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    *count = h;
+    return HG_OK;
+}
+
+int hg_world_poison_scratch(hg_world* w) {
+    HG_CHECK_WORLD(w);
+    DeviceGuard g(w->device);
+    const size_t b = cells(w) * sizeof(float);
+    for (int f = 0; f < S_COUNT; ++f) HG_CUDA(cudaMemsetAsync(w->alt[f], 0xFF, b, w->stream));
+    for (float* p : {w->u, w->v, w->vz, w->s_ero, w->b_ero, w->dirt[1], w->sdirt[1]})
+        if (p) HG_CUDA(cudaMemsetAsync(p, 0xFF, b, w->stream));
+    for (float4* p : {w->tc, w->td})
+        if (p) HG_CUDA(cudaMemsetAsync(p, 0xFF, 4 * b, w->stream));
     return HG_OK;
 }
 
@@ -1251,6 +1318,7 @@ int fused2_steps(hg_world* w, int nsteps) {
 }  // namespace
 
 int hg_step(hg_world* w, int nsteps, int mode) {
+    Range nv_range("hg_step");
     HG_CHECK_WORLD(w);
     if (nsteps < 0) return fail(HG_ERR_INVALID, "nsteps must be >= 0");
     if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_PARTICLES)
@@ -1436,6 +1504,7 @@ int hg_batch_destroy(hg_batch* b) {
 }
 
 int hg_batch_step(hg_batch* b, int nsteps, int mode) {
+    Range nv_range("hg_batch_step");
     if (!b) return fail(HG_ERR_INVALID, "null batch");
     if (nsteps < 0) return fail(HG_ERR_INVALID, "nsteps must be >= 0");
     if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_FUSED_PER_WORLD)
@@ -1500,6 +1569,11 @@ int hg_batch_step(hg_batch* b, int nsteps, int mode) {
         double best = 1e30;
         for (double m : b->tuning.ms) best = std::min(best, m);
         b->tuning.per_world = b->tuning.ms_per_world < best ? 1 : 0;
+        char m[120];
+        std::snprintf(m, sizeof m, "autotuner: batch of %zu worlds, %s (%.4f ms/step per world's launches)",
+                      b->worlds.size(), b->tuning.per_world ? "per-world launches" : "one table launch",
+                      b->tuning.ms_per_world);
+        log_msg(HG_LOG_INFO, m);
         if ((rc = release_worlds()) != HG_OK) return rc;
     }
     if (autotune && b->tuning.per_world) return per_world(nsteps);
@@ -1749,6 +1823,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
 }
 
 int hg_forward(hg_tape* t) {
+    Range nv_range("hg_forward");
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     hg_world* w = t->w;
     if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0) or the reference rain");
@@ -1782,6 +1857,7 @@ int hg_forward(hg_tape* t) {
 }
 
 int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* dL_drock0) {
+    Range nv_range("hg_backward");
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
     if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
@@ -1953,6 +2029,7 @@ struct FitScratch {
 
 int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, const hg_fit_settings* s,
                    double* losses, double* grad_norms) {
+    Range nv_range("hg_inverse_fit");
     HG_CHECK_WORLD(w);
     if (!s) return fail(HG_ERR_INVALID, "null fit settings");
     if (!target || !rock0 || !losses) return fail(HG_ERR_INVALID, "null target, initial rock or losses");
@@ -2051,6 +2128,7 @@ std::vector<int> ckpt_fields(int layers, bool ks_on) {
 }  // namespace
 
 int hg_world_save(hg_world* w, const char* path) {
+    Range nv_range("hg_world_save");
     HG_CHECK_WORLD(w);
     if (!path) return fail(HG_ERR_INVALID, "null path");
     DeviceGuard g(w->device);
@@ -2110,6 +2188,7 @@ int hg_world_save(hg_world* w, const char* path) {
 }
 
 int hg_world_load(hg_world* w, const char* path) {
+    Range nv_range("hg_world_load");
     HG_CHECK_WORLD(w);
     if (!path) return fail(HG_ERR_INVALID, "null path");
     DeviceGuard g(w->device);

@@ -94,6 +94,10 @@ class FitSettings(ctypes.Structure):
                 ("rock_step", ctypes.c_float)]
 
 
+# hg_log_fn: level (0 error, 1 info), message, user pointer
+LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p)
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"{LIB_PATH} is missing: build it with hydro-gen_gb300/build.py (no CPU fallback)")
@@ -159,6 +163,9 @@ def _load():
         "hg_backward": (ctypes.c_int, [P, P, P, P]),
         "hg_mse": (ctypes.c_int, [P, P, ctypes.POINTER(ctypes.c_double), P]),
         "hg_default_fit_settings": (ctypes.c_int, [ctypes.POINTER(FitSettings)]),
+        "hg_set_log_callback": (ctypes.c_int, [LOG_FN, P]),
+        "hg_world_poison_scratch": (ctypes.c_int, [P]),
+        "hg_world_count_nonfinite": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         "hg_inverse_fit": (ctypes.c_int, [P, P, P, P, ctypes.POINTER(FitSettings), ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double)]),
         "hg_world_save": (ctypes.c_int, [P, ctypes.c_char_p]),
@@ -462,6 +469,17 @@ def mse(world, target_ptr, grad_ptr=None):
     loss = ctypes.c_double()
     check(lib.hg_mse(world.h, ctypes.c_void_p(target_ptr), ctypes.byref(loss), ctypes.c_void_p(grad_ptr or 0)))
     return loss.value
+
+
+_log_keep = None
+
+
+def set_log(fn):
+    """Route the library's reports (hg_set_log_callback) to fn(level, text);
+    None turns them off.  Level 0 is a failure, 1 an autotuner choice."""
+    global _log_keep
+    _log_keep = LOG_FN(lambda level, msg, user: fn(level, msg.decode())) if fn else LOG_FN()
+    check(lib.hg_set_log_callback(_log_keep, None))
 
 
 def fit_settings(**kw):

@@ -175,6 +175,16 @@ typedef struct hg_world hg_world;
 const char* hg_version(void);
 /* Message of the last failed call on this thread ("" if none). */
 const char* hg_last_error(void);
+
+/* Host log hook (no counterpart in the reference, whose LOG / LOG_ERR macros
+ * print to stdout, src/utils.hpp:52-66): the library reports every failure
+ * (HG_LOG_ERROR, the text hg_last_error returns) and its autotuner's choices
+ * (HG_LOG_INFO) by calling fn(level, message, user) on the calling thread.
+ * NULL (the default) turns it off.  The message is valid during the call. */
+#define HG_LOG_ERROR 0
+#define HG_LOG_INFO 1
+typedef void (*hg_log_fn)(int level, const char* msg, void* user);
+int hg_set_log_callback(hg_log_fn fn, void* user);
 /* Number of kernels this library has launched in the process. */
 uint64_t hg_launch_count(void);
 
@@ -473,6 +483,16 @@ int hg_selftest_division(uint64_t seed, uint64_t count, uint64_t* mismatches);
  * so 2^18 * ns_per_poll bounds a kernel's wait for a lost tile (about 1 s).  The device
  * stays usable afterwards.  Synchronises. */
 int hg_selftest_bounded_wait(uint32_t polls, int* timed_out, double* ns_per_poll);
+/* Coverage checks.  hg_world_poison_scratch fills every buffer a step writes
+ * before reading (the alternate state buffers, velocity, the fused step's
+ * hand-off and the thermal scratch) with NaN; hg_world_count_nonfinite
+ * counts NaN and infinite values over the carried fields (rock, water,
+ * sediment, four fluxes, u, v; dirt and dirt sediment in two-layer worlds).
+ * After a step on a poisoned world the count is 0 exactly when the step
+ * wrote every cell it owns.  Both are ordered on the world's stream; the
+ * count synchronises. */
+int hg_world_poison_scratch(hg_world* w);
+int hg_world_count_nonfinite(hg_world* w, uint64_t* count);
 
 #ifdef __cplusplus
 }

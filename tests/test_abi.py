@@ -74,6 +74,21 @@ def test_error_paths_without_a_device(hg):
     assert hg.lib.hg_inverse_fit(None, None, None, None, ctypes.byref(fs), None, None) == -1
 
 
+def test_log_callback_receives_failures(hg):
+    got = []
+    hg.set_log(lambda level, text: got.append((level, text)))
+    try:
+        h = ctypes.c_void_p()
+        assert hg.lib.hg_world_create(12, 1, ctypes.byref(h)) == -1
+        assert got and got[-1][0] == 0 and "multiple of 8" in got[-1][1]
+        assert got[-1][1] == hg.lib.hg_last_error().decode()
+    finally:
+        hg.set_log(None)
+    n = len(got)
+    assert hg.lib.hg_world_create(12, 1, ctypes.byref(ctypes.c_void_p())) == -1
+    assert len(got) == n  # off again
+
+
 def test_header_cites_reference():
     text = open(os.path.join(ROOT, "include", "hydrogen.h")).read()
     for cite in ("glsl/bindings.glsl:39-60", "src/erosion.cpp", "src/state.cpp:116-147"):

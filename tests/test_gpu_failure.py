@@ -33,3 +33,50 @@ def test_bounded_wait_gives_up_and_the_device_stays_usable():
     for f in ("rock", "water", "sediment"):
         assert np.array_equal(a.download(f), b.download(f)), f
     b.sync()  # no tile of the fused steps timed out
+
+
+def two_layer_world(n):
+    s = H.ErosionSettings()
+    H.check(H.lib.hg_default_erosion_settings(ctypes.byref(s)))
+    w = H.World(n, layers=2)
+    w.init_reference_heightmap(H.map_settings(hmap_dims=(n, n)))
+    w.set_erosion(s)
+    w.set_rain(H.rain_uniform(0.01, 1))
+    w.set_options(H.options(H.RAIN_UNIFORM))
+    return w
+
+
+def one_layer_world(n, smooth=False):
+    w = H.World(n)
+    w.init_heightmap(H.noise(seed=5))
+    H.configure(w, "config2")
+    if smooth:
+        s = H.settings_config2()
+        s.Kspeed[1] = 1.0
+        w.set_erosion(s)
+    return w
+
+
+@pytest.mark.parametrize("layers,smooth,mode", [(1, False, H.MODE_PLAIN), (1, False, H.MODE_FUSED),
+                                                (1, True, H.MODE_FUSED), (2, False, H.MODE_PLAIN),
+                                                (2, False, H.MODE_FUSED)])
+def test_every_output_cell_is_written(layers, smooth, mode):
+    """Before each step every buffer the step writes is filled with NaN; after
+    it no carried field holds a NaN and the fields equal a world stepped
+    without poison, bit for bit: no cell is left unwritten or read before
+    it is written (192 = 3 x 64: edge and interior tiles)."""
+    n = 192
+    make = (lambda: two_layer_world(n)) if layers == 2 else (lambda: one_layer_world(n, smooth))
+    a, b = make(), make()
+    bad = ctypes.c_uint64()
+    for _ in range(3):
+        H.check(H.lib.hg_world_poison_scratch(b.h))
+        b.step(1, mode)
+        H.check(H.lib.hg_world_count_nonfinite(b.h, ctypes.byref(bad)))
+        assert bad.value == 0
+    a.step(3, mode)
+    fields = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b"]
+    if layers == 2:
+        fields += ["dirt", "sediment_dirt"]
+    for f in fields:
+        assert np.array_equal(a.download(f), b.download(f)), f
