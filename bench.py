@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
     ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint", "adjoint_thermal",
-                                        "config1"],
+                                        "batch", "config1"],
                     default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
@@ -728,6 +728,8 @@ def main():
             elif args.extra == "adjoint":  # --steps reversed steps, --warmup timed repetitions
                 out = bench_adjoint(H, torch, nsteps=args.steps, ckpt=min(32, args.steps),
                                     reps=max(1, args.warmup))
+            elif args.extra == "batch":  # --steps timed steps, --warmup warm-up steps
+                out = bench_batch(H, torch, nsteps=args.steps, warmup=args.warmup)
             elif args.extra == "adjoint_thermal":  # --n grid, --steps taped steps, --warmup repetitions
                 out = bench_adjoint_workload(H, torch, n=args.n, nsteps=args.steps, reps=max(1, args.warmup))
             else:
