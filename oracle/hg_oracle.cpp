@@ -142,7 +142,16 @@ inline float poly_atanf(float x) {
     else r = 1.57079637f - poly_atan_core(1.0f / ax);
     return std::copysign(r, x);
 }
-inline float o_atan(float x) { return poly_atanf(x); }
+// The float instantiation's arctangent: 0 = poly_atanf (the kernels' own,
+// for bit parity), 1 = the C library's atanf.  The second exists only to
+// measure how far the choice of arctangent moves the float result from FP64.
+static int g_float_atan_libm = 0;
+inline float o_atan(float x) { return g_float_atan_libm ? std::atan(x) : poly_atanf(x); }
+// Depth below which the flux pass sets the velocity to 0 (both
+// instantiations); 0 (the default) is the reference's scheme.  Exists only to
+// measure how much of the float-vs-FP64 distance the velocity of thin water
+// films (old-flux difference / depth) accounts for.
+static double g_film_guard = 0.0;
 inline double o_atan(double x) { return std::atan(x); }
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ---------------------
@@ -290,7 +299,7 @@ template <typename T> void flux_pass(World<T>& w, const OracleErosion& s) {
             terrain.z = d2;
             terrain.w = terrain.x + d2 + terrain.y;
             vel.z = d1 + d2;
-            if (vel.z > 0) {
+            if (vel.z > 0 && !(vel.z < T(g_film_guard))) {
                 vel.x = (gf(x - 1, y).y - gf(x, y).x + gf(x, y).y - gf(x + 1, y).x) / (L * vel.z);
                 vel.y = (gf(x, y - 1).z - gf(x, y).w + gf(x, y).z - gf(x, y + 1).w) / (L * vel.z);
             } else {
@@ -1026,6 +1035,21 @@ void hgo_totals(void* p, double out[4]) {
 }
 
 float hgo_atanf(float x) { return poly_atanf(x); }
+
+// Sets the film guard depth (see g_film_guard); returns the previous one.
+double hgo_set_film_guard(double depth) {
+    double prev = g_film_guard;
+    g_film_guard = depth;
+    return prev;
+}
+
+// Selects the float instantiation's arctangent (see o_atan); returns the
+// previous choice.
+int hgo_set_float_atan_libm(int on) {
+    int prev = g_float_atan_libm;
+    g_float_atan_libm = on ? 1 : 0;
+    return prev;
+}
 
 // Counts decreasing steps of poly_atanf over consecutive floats whose bit
 // patterns lie in [lo_bits, hi_bits] (non-negative floats order like their bits).

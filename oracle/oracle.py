@@ -71,6 +71,8 @@ def _load():
         "hgo_get_thermal": (ctypes.c_int, [P, P, P]),
         "hgo_totals": (None, [P, ctypes.POINTER(ctypes.c_double)]),
         "hgo_atanf": (ctypes.c_float, [ctypes.c_float]),
+        "hgo_set_float_atan_libm": (ctypes.c_int, [ctypes.c_int]),
+        "hgo_set_film_guard": (ctypes.c_double, [ctypes.c_double]),
         "hgo_philox4x32_10": (None, [ctypes.POINTER(ctypes.c_uint32)] * 3),
         "hgo_atan_monotone_violations": (ctypes.c_uint64, [ctypes.c_uint32, ctypes.c_uint32]),
         "hgo_rain_word": (ctypes.c_uint32, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32,
@@ -239,6 +241,36 @@ class OracleWorld:
 
 def atanf(x):
     return lib.hgo_atanf(x)
+
+
+class libm_atan:
+    """Context in which the float oracle takes its arctangent from the C
+    library (atanf) instead of the kernels' polynomial; for measuring how
+    much the arctangent moves the float result, never for parity."""
+
+    def __enter__(self):
+        self.prev = lib.hgo_set_float_atan_libm(1)
+        return self
+
+    def __exit__(self, *a):
+        lib.hgo_set_float_atan_libm(self.prev)
+
+
+class film_guard:
+    """Context in which the oracle's flux pass sets the velocity to 0 where
+    the depth d1 + d2 is below `depth` (both precisions): a change to the
+    scheme, for measuring how much of the float-vs-FP64 distance comes from
+    the velocity of thin films, never for parity."""
+
+    def __init__(self, depth):
+        self.depth = depth
+
+    def __enter__(self):
+        self.prev = lib.hgo_set_film_guard(self.depth)
+        return self
+
+    def __exit__(self, *a):
+        lib.hgo_set_film_guard(self.prev)
 
 
 def rain_word(x, y, step, terrain, seed):
