@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
     ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint", "adjoint_thermal",
-                                        "batch", "config1", "fp64_error"],
+                                        "batch", "config1", "fp64_error", "fit_study"],
                     default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
@@ -161,7 +161,44 @@ def cpu_baseline(n_sample=1024, budget_s=12.0):
                       f"(float oracle, OpenMP over rows)"}
 
 
-def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fit_iters=8):
+def fd_check(H, torch, w, tape, reset, b0, target, n, nsteps, g, dks, db0, cells=64, eps=1e-3, seed=0):
+    """The GPU adjoint's gradients at the fit's starting point (uniform Ks
+    0.05, the initial rock) against central finite differences of the FP64
+    reference forward (eps 1e-3) on `cells` random cells (fixed seed), for
+    both the per-cell Ks and the initial rock.  The FP64 differences run on
+    all host cores (each perturbed forward only where it differs from an
+    unperturbed one run in lockstep, bit for bit the full forward).
+    Relative error |g - fd| / max(|fd|, 1e-2 max|g|): the floor keeps cells
+    whose gradient is ~0 (deposition, where Ks has no effect) from dividing
+    by noise."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    ks = np.full((n, n), 0.05, np.float32)
+    w.upload("ks", ks)
+    reset()
+    tape.forward()
+    loss = H.mse(w, target.data_ptr(), g.data_ptr())
+    tape.backward(g.data_ptr(), dks.data_ptr(), db0.data_ptr())
+    w.sync()
+    gk, gb = dks.cpu().numpy().astype(np.float64), db0.cpu().numpy().astype(np.float64)
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(n * n, size=cells, replace=False)
+    t0 = time.perf_counter()
+    fd = O.fd_ref(O.settings_config1(), 0.01, 1, b0.astype(np.float64), ks, target.cpu().numpy().astype(np.float64),
+                  nsteps, np.concatenate([pick, pick]), np.array([0] * cells + [1] * cells), eps)
+    el = time.perf_counter() - t0
+    out = {"cells": cells, "eps": eps, "seed": seed, "loss": loss, "fd_seconds": el, "fd_cores": O.num_threads(),
+           "tolerance": 1e-3, "relative_error": "|g - fd| / max(|fd|, 1e-2 max|g|)"}
+    for name, grad, fdv in (("ks", gk, fd[:cells]), ("rock0", gb, fd[cells:])):
+        gv = grad.flat[pick]
+        rel = np.abs(gv - fdv) / np.maximum(np.abs(fdv), 1e-2 * np.abs(grad).max())
+        out[name] = {"within_tol": int(np.sum(rel <= 1e-3)), "max_rel": float(rel.max()),
+                     "median_rel": float(np.median(rel)), "max_abs_grad": float(np.abs(grad).max())}
+    w.sync()
+    return out
+
+
+def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fd_cells=64, fit_kw=None):
     """Forward + adjoint of the inverse-erosion workload: 1024^2, config-1
     physics, per-cell Ks = 0.05 exp(0.5 n(x)) from 3-octave simplex noise,
     MSE to a target, gradients for Ks and the initial rock; then fit_iters
@@ -170,6 +207,7 @@ def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fit_iters=8):
     w.init_heightmap(H.noise(seed=0))
     H.configure(w, "config1")
     w.init_ks_field(H.noise(seed=7, octaves=3, frequency=1.0 / 256), 0.05, 0.5)
+    ks_true = w.download("ks")
     w.step(nsteps, H.MODE_FUSED)
     target = torch.empty((n, n), dtype=torch.float32, device="cuda")
     w.download_device("rock", target.data_ptr())
@@ -203,21 +241,63 @@ def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fit_iters=8):
             all_ms.append(e0.elapsed_time(e2))
     f, a = statistics.median(fwd_ms), statistics.median(all_ms)
     cs = n * n * nsteps
-    # the fit itself, through hg_inverse_fit from uniform Ks = 0.05 and the
-    # true initial rock: wall time of the whole call (tape and scratch set-up included)
-    ks = torch.full((n, n), 0.05, dtype=torch.float32, device="cuda")
-    b0_dev = torch.from_numpy(b0).cuda()
-    fs = H.fit_settings(nsteps=nsteps, ckpt_every=ckpt, iters=fit_iters, ks_step=0.01, rock_step=0.02)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    losses, norms = H.inverse_fit(w, target.data_ptr(), ks.data_ptr(), b0_dev.data_ptr(), fs, grad_norms=True)
-    fit_s = time.perf_counter() - t0
+    fd = fd_check(H, torch, w, tape, reset, b0, target, n, nsteps, g, dks, db0) if fd_cells else None
+    # the fit itself (hg_inverse_fit) from uniform Ks = 0.05 and the true
+    # initial rock
+    fit = bench_fit(H, torch, w, target, ks_true, b0, n, nsteps, ckpt, **(fit_kw or {}))
     return {"workload": f"inverse erosion {n}x{n}, {nsteps} steps, per-cell Ks, checkpoints every {ckpt}",
             "forward_cell_steps_per_s": cs / (f / 1e3), "fwd_adjoint_cell_steps_per_s": cs / (a / 1e3),
             "fwd_adjoint_over_forward_time": a / f, "ms_forward": f, "ms_fwd_adjoint": a,
-            "fit": {"iters": fit_iters, "ks_step": 0.01, "rock_step": 0.02, "ms_per_iter": fit_s * 1e3 / fit_iters,
-                    "loss_first": losses[0], "loss_last": losses[-1], "grad_norm_first": norms[0],
-                    "grad_norm_last": norms[-1]}}
+            "fd_check": fd, "fit": fit}
+
+
+def bench_fit(H, torch, w, target, ks_true, b0, n, nsteps, ckpt, iters=100, chunk=10, ks_step=0.01,
+              rock_step=0.0, decay=0.8):
+    """The inverse-erosion fit of the 1024^2 workload through hg_inverse_fit:
+    from uniform Ks = 0.05 (and the true initial rock), `iters` iterations
+    in calls of `chunk`, the largest per-iteration change multiplied by
+    `decay` after each call (a normalised descent with a fixed step stalls
+    at a step-sized oscillation).  Reports the loss of every iteration, and
+    after every call the relative L2 error of the fitted Ks against the
+    target's Ks field, over all cells and over the cells where the first
+    gradient moved Ks (erosion happens there; elsewhere the loss does not
+    depend on Ks and Ks keeps its start value), and the RMS error of the
+    initial rock (height units)."""
+    ks = torch.full((n, n), 0.05, dtype=torch.float32, device="cuda")
+    b0_dev = torch.from_numpy(b0).cuda()
+    b0_true = b0_dev.clone()
+    kt = torch.from_numpy(ks_true).cuda().double()
+    losses, norms, curve = [], [], []
+    moved = None
+    ms = 0.0
+    step_k, step_b = ks_step, rock_step
+    for c0 in range(0, iters, chunk):
+        k = min(chunk, iters - c0)
+        fs = H.fit_settings(nsteps=nsteps, ckpt_every=ckpt, iters=k, ks_step=step_k, rock_step=step_b)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        l, g = H.inverse_fit(w, target.data_ptr(), ks.data_ptr(), b0_dev.data_ptr(), fs, grad_norms=True)
+        ms += (time.perf_counter() - t0) * 1e3
+        losses += l
+        norms += g
+        if moved is None:
+            moved = ks != 0.05
+        d = ks.double() - kt
+        curve.append({"iter": c0 + k, "ks_step": step_k, "loss": l[-1],
+                      "ks_rel_err": float(d.norm() / kt.norm()),
+                      "ks_rel_err_eroding": float(d[moved].norm() / kt[moved].norm()) if bool(moved.any()) else None,
+                      "rock0_rms_err": float((b0_dev.double() - b0_true.double()).pow(2).mean().sqrt())})
+        step_k *= decay
+        step_b *= decay
+    d0 = torch.full_like(kt, 0.05) - kt
+    return {"iters": iters, "chunk": chunk, "ks_step": ks_step, "rock_step": rock_step, "decay": decay,
+            "ms_per_iter": ms / iters, "losses": losses, "grad_norms": norms,
+            "ks_rel_err_start": float(d0.norm() / kt.norm()),
+            "ks_rel_err_start_eroding": float(d0[moved].norm() / kt[moved].norm()) if bool(moved.any()) else None,
+            "eroding_cells": int(moved.sum()), "curve": curve,
+            "ks_rel_err": curve[-1]["ks_rel_err"], "ks_rel_err_eroding": curve[-1]["ks_rel_err_eroding"],
+            "rock0_rms_err": curve[-1]["rock0_rms_err"],
+            "loss_first": losses[0], "loss_last": losses[-1]}
 
 
 def bench_adjoint_workload(H, torch, n=N_GRID, nsteps=100, reps=2):
@@ -785,6 +865,15 @@ def main():
                 out = bench_config1(H, torch, cpu=budget > 0)
             elif args.extra == "fp64_error":
                 out = bench_fp64_error(H, torch)
+            elif args.extra == "fit_study":  # fit schedules on the inverse workload
+                out = {}
+                for name, kw in (("ks_fixed_0.01", dict(ks_step=0.01, decay=1.0)),
+                                 ("ks_0.01_decay_0.8", dict(ks_step=0.01, decay=0.8)),
+                                 ("ks_0.005_decay_0.9", dict(ks_step=0.005, decay=0.9)),
+                                 ("ks_rock_0.01_0.02_decay_0.8", dict(ks_step=0.01, rock_step=0.02, decay=0.8))):
+                    r = bench_adjoint(H, torch, reps=1, fd_cells=0, fit_kw=kw)["fit"]
+                    out[name] = {k: v for k, v in r.items() if k not in ("losses", "grad_norms")}
+                    out[name]["losses_every_10"] = r["losses"][::10] + [r["losses"][-1]]
             elif args.extra == "adjoint":  # --steps reversed steps, --warmup timed repetitions
                 out = bench_adjoint(H, torch, nsteps=args.steps, ckpt=min(32, args.steps),
                                     reps=max(1, args.warmup))

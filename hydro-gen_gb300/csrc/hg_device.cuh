@@ -26,7 +26,8 @@ __device__ __forceinline__ float gmix(float x, float y, float a) { return x * (1
 // (glsl/hydro_flux.glsl:36, glsl/thermal_erosion.glsl:23): 999999999999.0 as float
 constexpr float FAR_HEIGHT = 999999995904.0f;
 
-// Single-precision arctangent (csrc/fit_atan.py): three branches keep the
+// Single-precision arctangent (coefficients from oracle/fit_atan.py, a Lawson
+// minimax fit): three branches keep the
 // polynomial argument within |u| <= tan(pi/8),
 //   x <= tan(pi/8): poly(x);  x <= tan(3pi/8): pi/4 + poly((x-1)/(x+1));
 //   else pi/2 - poly(1/x);    poly(u) = u + u*(s*P(s)), s = u*u.

@@ -10,6 +10,8 @@
 #include <cstdio>
 #include <cstring>
 #include <array>
+#include <memory>
+#include <mutex>
 #include <new>
 #include <vector>
 #include <string>
@@ -107,6 +109,7 @@ struct hg_world {
     float* s_ero = nullptr;  // fused step: eroded sediment of every cell
     float* b_ero = nullptr;  // fused step: eroded rock of every cell
     int* err = nullptr;      // device flag: a bounded wait gave up
+    bool invalid = false;    // a sync saw that flag: fields undefined until re-initialised or loaded
     unsigned long long* d_step = nullptr;  // device copy of `step`, advanced by the fused kernels
     bool dev_step_valid = false;           // d_step == step
     uint64_t version = 1;                  // bumps whenever settings, options or Ks change
@@ -171,12 +174,21 @@ namespace {
 
 thread_local std::string t_err;
 
-// the host log hook (hg_set_log_callback); set rarely, read on every report
-std::atomic<hg_log_fn> g_log_fn{nullptr};
-std::atomic<void*> g_log_user{nullptr};
+// The host log hook (hg_set_log_callback): set rarely, read on every
+// report.  The (function, user) pair is published as one pointer to an
+// immutable record, so a report never pairs a new function with an old
+// user pointer; records stay alive until exit (a reader may still hold one).
+struct LogHook {
+    hg_log_fn fn;
+    void* user;
+};
+std::atomic<const LogHook*> g_log{nullptr};
+std::mutex g_log_mu;
+std::vector<std::unique_ptr<LogHook>> g_log_hooks;  // every record ever published
 
 void log_msg(int level, const std::string& msg) {
-    if (hg_log_fn fn = g_log_fn.load(std::memory_order_acquire)) fn(level, msg.c_str(), g_log_user.load());
+    if (const LogHook* h = g_log.load(std::memory_order_acquire))
+        if (h->fn) h->fn(level, msg.c_str(), h->user);
 }
 
 int fail(int code, const std::string& msg) {
@@ -205,6 +217,13 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 #define HG_CHECK_WORLD(w) \
     if (!(w)) return fail(HG_ERR_INVALID, "null world")
+
+// Entry points that advance or read a world's state refuse a world whose
+// fields a timed-out tile load left undefined.
+#define HG_CHECK_VALID(w)                                                                      \
+    if ((w)->invalid)                                                                          \
+    return fail(HG_ERR_TIMEOUT, "the world's fields are undefined after a timed-out tile load; " \
+                                "re-initialise it (hg_init_heightmap, hg_init_reference_heightmap) or load it")
 
 // Make the world's device current for the duration of a call.
 struct DeviceGuard {
@@ -661,8 +680,9 @@ const char* hg_version(void) { return "hydrogen-gb300 0.1 (sm_103a)"; }
 const char* hg_last_error(void) { return t_err.c_str(); }
 
 int hg_set_log_callback(hg_log_fn fn, void* user) {
-    g_log_user.store(user, std::memory_order_relaxed);
-    g_log_fn.store(fn, std::memory_order_release);
+    std::lock_guard<std::mutex> lk(g_log_mu);
+    g_log_hooks.push_back(std::unique_ptr<LogHook>(new LogHook{fn, user}));
+    g_log.store(fn ? g_log_hooks.back().get() : nullptr, std::memory_order_release);
     return HG_OK;
 }
 uint64_t hg_launch_count(void) { return g_launches.load(); }
@@ -951,6 +971,7 @@ int hg_init_reference_heightmap(hg_world* w, const hg_map_settings* s) {
     w->version += 1;
     w->step = 0;
     w->dev_step_valid = false;
+    w->invalid = false;
     return HG_OK;
 }
 
@@ -1047,6 +1068,7 @@ int hg_render(hg_world* w, const hg_camera* cam, int width, int height, uint8_t*
 
 int hg_rain(hg_world* w, float time) {
     HG_CHECK_WORLD(w);
+    HG_CHECK_VALID(w);
     DeviceGuard g(w->device);
     if (w->opt.rain_mode == HG_RAIN_OFF) return HG_OK;
     if (w->opt.rain_mode == HG_RAIN_REFERENCE) {
@@ -1154,6 +1176,7 @@ int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
     HG_CUDA(cudaGetLastError());
     w->step = 0;
     w->dev_step_valid = false;
+    w->invalid = false;
     return HG_OK;
 }
 
@@ -1320,6 +1343,7 @@ int fused2_steps(hg_world* w, int nsteps) {
 int hg_step(hg_world* w, int nsteps, int mode) {
     Range nv_range("hg_step");
     HG_CHECK_WORLD(w);
+    HG_CHECK_VALID(w);
     if (nsteps < 0) return fail(HG_ERR_INVALID, "nsteps must be >= 0");
     if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_PARTICLES)
         return fail(HG_ERR_INVALID, "bad mode");
@@ -1510,6 +1534,7 @@ int hg_batch_step(hg_batch* b, int nsteps, int mode) {
     if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_FUSED_PER_WORLD)
         return fail(HG_ERR_INVALID, "bad mode");
     if (nsteps == 0) return HG_OK;
+    for (hg_world* w : b->worlds) HG_CHECK_VALID(w);
     DeviceGuard g(b->device);
     bool two_layer = false;  // the table launch covers one-layer worlds
     for (hg_world* w : b->worlds) two_layer = two_layer || w->layers == 2;
@@ -1593,7 +1618,9 @@ int hg_batch_sync(hg_batch* b) {
     HG_CUDA(cudaMemcpy(&flag, b->err, sizeof(int), cudaMemcpyDeviceToHost));
     if (flag) {
         HG_CUDA(cudaMemset(b->err, 0, sizeof(int)));
-        return fail(HG_ERR_TIMEOUT, "a fused-step tile load did not arrive within its bounded wait");
+        for (hg_world* w : b->worlds) w->invalid = true;
+        return fail(HG_ERR_TIMEOUT, "a fused-step tile load did not arrive within its bounded wait; "
+                                    "the batch's fields are undefined until its worlds are re-initialised or loaded");
     }
     for (hg_world* w : b->worlds) {
         int rc = hg_sync(w);
@@ -1632,8 +1659,9 @@ int hg_sync(hg_world* w) {
     HG_CUDA(cudaMemcpy(&flag, w->err, sizeof(int), cudaMemcpyDeviceToHost));
     if (flag) {
         HG_CUDA(cudaMemset(w->err, 0, sizeof(int)));
+        w->invalid = true;
         return fail(HG_ERR_TIMEOUT, "a fused-step tile load did not arrive within its bounded wait; "
-                                    "the step's fields are not valid");
+                                    "the world's fields are undefined until it is re-initialised or loaded");
     }
     return HG_OK;
 }
@@ -1826,6 +1854,7 @@ int hg_forward(hg_tape* t) {
     Range nv_range("hg_forward");
     if (!t) return fail(HG_ERR_INVALID, "null tape");
     hg_world* w = t->w;
+    HG_CHECK_VALID(w);
     if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0) or the reference rain");
     DeviceGuard g(w->device);
     t->step0 = w->step;
@@ -2033,6 +2062,7 @@ int hg_inverse_fit(hg_world* w, const float* target, float* ks, float* rock0, co
     HG_CHECK_WORLD(w);
     if (!s) return fail(HG_ERR_INVALID, "null fit settings");
     if (!target || !rock0 || !losses) return fail(HG_ERR_INVALID, "null target, initial rock or losses");
+    HG_CHECK_VALID(w);
     if (s->iters < 1) return fail(HG_ERR_INVALID, "iters must be >= 1");
     if (!(s->ks_step >= 0.0f) || !(s->rock_step >= 0.0f)) return fail(HG_ERR_INVALID, "steps must be >= 0");
     if (s->ks_step > 0.0f && !ks) return fail(HG_ERR_INVALID, "fitting Ks needs a Ks buffer");
@@ -2262,6 +2292,16 @@ int hg_world_load(hg_world* w, const char* path) {
     w->ks_on = h.ks_on != 0;
     w->dev_step_valid = false;
     w->version += 1;
+    w->invalid = false;
+    return HG_OK;
+}
+
+int hg_selftest_report_timeout(hg_world* w) {
+    HG_CHECK_WORLD(w);
+    DeviceGuard g(w->device);
+    const int one = 1;  // what a kernel's bounded wait writes when it gives up
+    HG_CUDA(cudaMemcpyAsync(w->err, &one, sizeof(int), cudaMemcpyHostToDevice, w->stream));
+    HG_CUDA(cudaStreamSynchronize(w->stream));
     return HG_OK;
 }
 

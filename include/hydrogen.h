@@ -335,7 +335,14 @@ int hg_step(hg_world* w, int nsteps, int mode);
 int hg_rain(hg_world* w, float time);
 /* Waits for the world's stream (the reference's glMemoryBarrier/glFinish).
  * HG_ERR_TIMEOUT if a fused-step tile load gave up its bounded wait since the
- * last sync (the step's fields are then not valid). */
+ * last sync.  After that error the world's fields are undefined: the block
+ * that gave up skipped its tile, and a copy it left in flight may still land
+ * in shared memory that a later block on the same SM owns, so every world
+ * stepped on the same device since the last good sync is suspect too.  The
+ * world then refuses hg_step, hg_rain, hg_forward and hg_inverse_fit with
+ * HG_ERR_TIMEOUT until hg_init_heightmap, hg_init_reference_heightmap or
+ * hg_world_load gives it defined fields again; reload the other worlds of
+ * the device from their last checkpoints as well. */
 int hg_sync(hg_world* w);
 /* Fused-step variant the autotuner chose for this world (tile height 16 or 8,
  * 0 before tuning; graph replay 0/1) and the candidates' ms per step in the
@@ -483,6 +490,11 @@ int hg_selftest_division(uint64_t seed, uint64_t count, uint64_t* mismatches);
  * so 2^18 * ns_per_poll bounds a kernel's wait for a lost tile (about 1 s).  The device
  * stays usable afterwards.  Synchronises. */
 int hg_selftest_bounded_wait(uint32_t polls, int* timed_out, double* ns_per_poll);
+/* Test hook (no counterpart in the reference): sets the world's device error
+ * flag from the host, as a kernel's bounded wait does when it gives up, so
+ * that the HG_ERR_TIMEOUT contract of hg_sync can be tested without a GPU
+ * fault or a real lost copy. */
+int hg_selftest_report_timeout(hg_world* w);
 /* Coverage checks.  hg_world_poison_scratch fills every buffer a step writes
  * before reading (the alternate state buffers, velocity, the fused step's
  * hand-off and the thermal scratch) with NaN; hg_world_count_nonfinite

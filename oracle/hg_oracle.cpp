@@ -40,7 +40,7 @@
 //
 // GLSL leaves atan's precision to the driver.  The float instantiation uses
 // the library's polynomial arctangent (coefficients from
-// hydro-gen_gb300/csrc/fit_atan.py, restated here) so that float results can
+// oracle/fit_atan.py, restated here) so that float results can
 // be compared bit for bit; the double instantiation uses std::atan.
 
 #include <cmath>

@@ -304,6 +304,14 @@ lib.hgo_adjoint_ref.restype = ctypes.c_int
 lib.hgo_adjoint_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                 ctypes.c_void_p, ctypes.c_void_p]
+lib.hgo_fd_ref.restype = ctypes.c_int
+lib.hgo_fd_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                           ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
+lib.hgo_fd_ref_final.restype = ctypes.c_int
+lib.hgo_fd_ref_final.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                 ctypes.c_void_p, ctypes.c_void_p]
 lib.hgo_forward_ref.restype = ctypes.c_int
 lib.hgo_forward_ref.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -416,6 +424,41 @@ def adjoint_ref(settings, amount, period, b0, ks, target, nsteps, step0=0):
                              ctypes.byref(loss), dks.ctypes.data, db0.ctypes.data)
     assert rc == 0
     return loss.value, dks, db0
+
+
+def fd_ref(settings, amount, period, b0, ks, target, nsteps, cells, params, eps, step0=0):
+    """Central finite differences of the FP64 reference's loss (mean squared
+    rock error after nsteps) for each (flat cell index, parameter) pair:
+    parameter 0 = the cell's Ks, 1 = its initial rock; pairs run in parallel
+    over the host's threads.  Returns dL/dparam per pair."""
+    n = b0.shape[0]
+    st = _adj_settings(settings, amount)
+    b0 = np.ascontiguousarray(b0, dtype=np.float64)
+    ks = np.ascontiguousarray(ks, dtype=np.float32)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    cells = np.ascontiguousarray(cells, dtype=np.int32)
+    params = np.ascontiguousarray(params, dtype=np.int32)
+    out = np.empty(len(cells))
+    rc = lib.hgo_fd_ref(n, st.ctypes.data, period, step0, nsteps, b0.ctypes.data, ks.ctypes.data, tg.ctypes.data,
+                        len(cells), cells.ctypes.data, params.ctypes.data, eps, out.ctypes.data)
+    assert rc == 0
+    return out
+
+
+def fd_ref_final(settings, amount, period, b0, ks, nsteps, cell, param, delta, step0=0):
+    """Final rock of fd_ref's windowed forward for one perturbation (flat
+    cell, parameter 0 = Ks / 1 = initial rock, signed delta) and the number
+    of cells its window grew to."""
+    n = b0.shape[0]
+    st = _adj_settings(settings, amount)
+    b0 = np.ascontiguousarray(b0, dtype=np.float64)
+    ks = np.ascontiguousarray(ks, dtype=np.float32)
+    out = np.empty((n, n))
+    rc_cells = ctypes.c_int()
+    rc = lib.hgo_fd_ref_final(n, st.ctypes.data, period, step0, nsteps, b0.ctypes.data, ks.ctypes.data, cell,
+                              param, delta, out.ctypes.data, ctypes.byref(rc_cells))
+    assert rc == 0
+    return out, rc_cells.value
 
 
 def forward_ref(settings, amount, period, b0, ks, nsteps, step0=0):

@@ -94,3 +94,43 @@ def test_reference_adjoint_vs_finite_differences(thermal):
     # switch; allow at most 2 of the 128 comparisons to do so
     print(f"thermal={thermal} eps={eps}: {len(bad)} of 128 outside 1e-3", bad[:3])
     assert len(bad) <= 2, bad[:5]
+
+
+@pytest.mark.parametrize("cell,param,delta", [(N * 17 + 9, 0, 1e-3), (N * 3 + 30, 1, -1e-3), (0, 1, 1e-3),
+                                              (N * N - 1, 0, -1e-3)])
+def test_windowed_fd_forward_is_the_full_forward(cell, param, delta):
+    """fd_ref runs each perturbed forward only where it differs from an
+    unperturbed one in lockstep; the result must be the full forward of the
+    perturbed inputs, bit for bit."""
+    _, b0, ks, _ = setup()
+    s = settings(False)
+    b2, k2 = b0.copy(), ks.copy()
+    if param == 0:
+        k2.flat[cell] = np.float32(float(ks.flat[cell]) + delta)
+    else:
+        b2.flat[cell] += delta
+    full = O.forward_ref(s, 0.01, 1, b2, k2, STEPS)
+    win, rect = O.fd_ref_final(s, 0.01, 1, b0, ks, STEPS, cell, param, delta)
+    assert np.array_equal(full, win)
+    assert rect < N * N
+
+
+def test_fd_ref_matches_direct_differences():
+    rng, b0, ks, target = setup()
+    s = settings(False)
+    cells = rng.choice(N * N, size=6, replace=False)
+    params = np.array([0, 1, 0, 1, 0, 1])
+    fd = O.fd_ref(s, 0.01, 1, b0, ks, target, STEPS, cells, params, 1e-3)
+    for c, p, g in zip(cells, params, fd):
+        b2p, b2m, kp, km = b0.copy(), b0.copy(), ks.copy(), ks.copy()
+        if p == 0:
+            kp.flat[c] = np.float32(float(ks.flat[c]) + 1e-3)
+            km.flat[c] = np.float32(float(ks.flat[c]) - 1e-3)
+            h = float(kp.flat[c]) - float(km.flat[c])
+        else:
+            b2p.flat[c] += 1e-3
+            b2m.flat[c] -= 1e-3
+            h = 2e-3
+        lp, lm = oracle_loss(b2p, kp, target), oracle_loss(b2m, km, target)
+        ref = (lp - lm) / h
+        assert abs(g - ref) <= 1e-6 * max(abs(ref), 1e-12), (c, p, g, ref)

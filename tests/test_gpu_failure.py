@@ -35,6 +35,36 @@ def test_bounded_wait_gives_up_and_the_device_stays_usable():
     b.sync()  # no tile of the fused steps timed out
 
 
+def test_timeout_leaves_the_world_undefined_until_reinitialised():
+    """hg_sync's HG_ERR_TIMEOUT contract, exercised without a lost copy: the
+    host sets the device flag a giving-up wait would set.  The world then
+    refuses to step until it is re-initialised, and steps again after."""
+    w = H.World(128)
+    w.init_heightmap(H.noise(seed=1))
+    H.configure(w, "config2")
+    w.step(4, H.MODE_FUSED)
+    w.sync()
+    H.check(H.lib.hg_selftest_report_timeout(w.h))
+    assert H.lib.hg_sync(w.h) == -4
+    for mode in (H.MODE_PLAIN, H.MODE_FUSED):
+        with pytest.raises(H.HydrogenError) as e:
+            w.step(1, mode)
+        assert e.value.code == -4
+    tape = H.Tape(w, 4, 4)
+    with pytest.raises(H.HydrogenError) as e:
+        tape.forward()
+    assert e.value.code == -4
+    tape.close()
+    w.init_heightmap(H.noise(seed=1))
+    w.step(4, H.MODE_FUSED)
+    w.sync()
+    ref = H.World(128)
+    ref.init_heightmap(H.noise(seed=1))
+    H.configure(ref, "config2")
+    ref.step(4, H.MODE_FUSED)
+    assert np.array_equal(w.download("rock"), ref.download("rock"))
+
+
 def two_layer_world(n):
     s = H.ErosionSettings()
     H.check(H.lib.hg_default_erosion_settings(ctypes.byref(s)))

@@ -100,8 +100,9 @@ def test_fused_tile_option(tile_y):
 
 def test_fused_far_backtrace_fallback():
     """Velocities of hundreds of cells per step send sediment back-traces far
-    outside the staged tile; the fused kernel recomputes those taps from the
-    step's input fields and must still match the per-pass kernels exactly."""
+    outside any tile; the fused transport kernel gathers those taps from the
+    eroded sediment that the hydro kernel wrote for every cell, and must
+    still match the per-pass kernels exactly."""
     n = 128
     rng = np.random.default_rng(3)
     state = {"rock": rng.random((n, n)) * 10, "water": np.full((n, n), 1e-3),
