@@ -252,12 +252,13 @@ def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fd_cells=64, fi
 
 
 def bench_fit(H, torch, w, target, ks_true, b0, n, nsteps, ckpt, iters=100, chunk=10, ks_step=0.01,
-              rock_step=0.0, decay=0.8):
+              rock_step=0.0, decay=1.0):
     """The inverse-erosion fit of the 1024^2 workload through hg_inverse_fit:
     from uniform Ks = 0.05 (and the true initial rock), `iters` iterations
     in calls of `chunk`, the largest per-iteration change multiplied by
-    `decay` after each call (a normalised descent with a fixed step stalls
-    at a step-sized oscillation).  Reports the loss of every iteration, and
+    `decay` after each call (1: a fixed step; on this workload a fixed step
+    of 0.01 lowered the loss and the Ks error further in 100 iterations than
+    steps shrinking by 0.8 or 0.9 per call).  Reports the loss of every iteration, and
     after every call the relative L2 error of the fitted Ks against the
     target's Ks field, over all cells and over the cells where the first
     gradient moved Ks (erosion happens there; elsewhere the loss does not

@@ -431,6 +431,189 @@ __device__ __forceinline__ void cell_thermal_outflows1(const StepConsts& c, cons
     cell_thermal_outflows_dh(c.dt, c.Kalpha1, c.Kspeed1, t.x_cross, t.b_diag, t.fast_div, g, dh, o);
 }
 
+// ---- two cells at once: paired FP32 arithmetic ----------------------------------
+// sm_100-class GPUs issue two independent IEEE single-precision adds,
+// multiplies or fused multiply-adds as one f32x2 instruction.  Each lane
+// rounds exactly as the scalar operation, so two cells evaluated in lanes .x
+// and .y keep the scalar cells' bits while the pair costs one issue slot.
+__device__ __forceinline__ float2 pf(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+// The multiply is a fused multiply-add of -0: a * b + (-0) is a * b
+// rounded once, signed zeros included.  The -0 pair sits in constant
+// memory, so the compiler cannot turn it back into a multiply instruction:
+// at -O3 ptxas contracts an f32x2 multiply that feeds an f32x2 add into one
+// fused multiply-add, even with .rn and --fmad=false (measured: a
+// two-product mix differed from the scalar one in a third of the lanes),
+// while a fused multiply-add feeding an add stays two roundings.
+static __constant__ float2 kNegZero2 = {-0.0f, -0.0f};
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return fma2(a, b, kNegZero2); }
+// a - b as b * (-1) + a: the product is exact, so this is one rounding of
+// a - b (signed zeros included)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return fma2(b, make_float2(-1.0f, -1.0f), a); }
+
+// div_recip on two lanes with nb = -b: fma(q, -b, a) is fma(-q, b, a)
+// exactly (the product's sign moves, nothing rounds differently).
+__device__ __forceinline__ float2 div_recip2(float2 a, float2 nb, float2 y) {
+    float2 q = mul2(a, y);
+    float2 r = fma2(q, nb, a);
+    q = fma2(r, y, q);
+    r = fma2(q, nb, a);
+    return fma2(r, y, q);
+}
+
+// poly_atanf of two non-negative arguments: the reduction's division runs
+// per lane, the polynomial on the pair.
+__device__ __forceinline__ float2 poly_atanf2(float2 x) {
+    const float c0 = -3.333333135e-01f, c1 = 1.999990344e-01f, c2 = -1.428200752e-01f,
+                c3 = 1.104469076e-01f, c4 = -8.476266265e-02f, c5 = 4.744043201e-02f;
+    const bool midx = x.x > 0.414213562f && x.x <= 2.41421356f, bigx = x.x > 2.41421356f;
+    const bool midy = x.y > 0.414213562f && x.y <= 2.41421356f, bigy = x.y > 2.41421356f;
+    float2 u = x;
+    if (midx || bigx) u.x = __fdiv_rn(midx ? __fsub_rn(x.x, 1.0f) : 1.0f, midx ? __fadd_rn(x.x, 1.0f) : x.x);
+    if (midy || bigy) u.y = __fdiv_rn(midy ? __fsub_rn(x.y, 1.0f) : 1.0f, midy ? __fadd_rn(x.y, 1.0f) : x.y);
+    const float2 s = mul2(u, u);
+    float2 p = pf(c5);
+    p = add2(mul2(p, s), pf(c4));
+    p = add2(mul2(p, s), pf(c3));
+    p = add2(mul2(p, s), pf(c2));
+    p = add2(mul2(p, s), pf(c1));
+    p = add2(mul2(p, s), pf(c0));
+    p = add2(u, mul2(u, mul2(s, p)));
+    const float2 pm = add2(pf(0.785398163f), p), pb = sub2(pf(1.57079637f), p);
+    return make_float2(midx ? pm.x : bigx ? pb.x : p.x, midy ? pm.y : bigy ? pb.y : p.y);
+}
+
+// cell_thermal_outflows_dh for two cells (lanes .x, .y) with the same
+// operations per lane; dm holds the drops on entry and is overwritten with
+// the marked drops (0 where unmarked: a marked drop equals its drop, so the
+// scalar fallback's S * dh reads it from there).  A lane with no marked
+// direction keeps its zeros; it runs the paired quotients on a divisor of 1
+// and a dividend of +0, whose quotient is +0, so the pair stays on one path.
+// Lanes whose operands leave div_recip's range take the scalar path of
+// cell_thermal_outflows_dh.
+__device__ __forceinline__ void cell_thermal_outflows_dh2(float dt, float Kalpha, float Kspeed, float x_cross,
+                                                          float b_diag, int fast_div, float2 terr, float2 dm[8],
+                                                          float2 o[8]) {
+    float Hx = 0.0f, Hy = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        Hx = fmaxf(Hx, dm[k].x);
+        Hy = fmaxf(Hy, dm[k].y);
+    }
+    const float2 H = make_float2(gmin(terr.x, Hx), gmin(terr.y, Hy));
+    float2 bk = pf(0.0f);
+    float mcx = 0.0f, mcy = 0.0f, mdx = 0.0f, mdy = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float t = k < 4 ? x_cross : b_diag;
+        dm[k] = make_float2(dm[k].x >= t ? dm[k].x : 0.0f, dm[k].y >= t ? dm[k].y : 0.0f);
+        bk = add2(bk, dm[k]);
+        if (k < 4) {
+            mcx = fmaxf(mcx, dm[k].x);
+            mcy = fmaxf(mcy, dm[k].y);
+        } else {
+            mdx = fmaxf(mdx, dm[k].x);
+            mdy = fmaxf(mdy, dm[k].y);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o[k] = pf(0.0f);
+    const bool mx = bk.x > 0.0f, my = bk.y > 0.0f;
+    if (!mx && !my) return;
+    bool fx = fast_div && bk.x <= 0x1p40f, fy = fast_div && bk.y <= 0x1p40f;
+    float2 sd;
+    if ((fx || !mx) && (fy || !my)) {
+        sd = div_recip2(make_float2(mdx, mdy), pf(-SQRT2_F), pf(RCP_SQRT2_F));
+    } else {
+        sd.x = fx ? div_recip(mdx, SQRT2_F, RCP_SQRT2_F) : mdx / SQRT2_F;
+        sd.y = fy ? div_recip(mdy, SQRT2_F, RCP_SQRT2_F) : mdy / SQRT2_F;
+    }
+    const float2 alph = poly_atanf2(make_float2(fmaxf(mcx, sd.x), fmaxf(mcy, sd.y)));
+    const float2 newsh = sub2(add2(pf(1.0f), alph), pf(Kalpha));
+    float2 sharp = make_float2(newsh.x > 1.0f ? newsh.x : 1.0f, newsh.y > 1.0f ? newsh.y : 1.0f);
+    sharp = mul2(sharp, mul2(sharp, sharp));
+    // dt * Kspeed * sharp * H / 2 (a == L == 1); halving is exact either way
+    const float2 S = mul2(mul2(mul2(pf(dt * Kspeed), sharp), H), pf(0.5f));
+    fx = fx && S.x >= 0x1p-50f && S.x <= 0x1p40f;
+    fy = fy && S.y >= 0x1p-50f && S.y <= 0x1p40f;
+    if ((fx || !mx) && (fy || !my)) {
+        const float2 b = make_float2(mx ? bk.x : 1.0f, my ? bk.y : 1.0f);
+        const float2 y = make_float2(__frcp_rn(b.x), __frcp_rn(b.y));
+        const float2 nb = make_float2(-b.x, -b.y);
+        const float2 S2 = make_float2(mx ? S.x : 0.0f, my ? S.y : 0.0f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o[k] = div_recip2(mul2(S2, dm[k]), nb, y);
+        return;
+    }
+    if (mx) {
+        if (fx) {
+            const float y = __frcp_rn(bk.x);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) o[k].x = div_recip(S.x * dm[k].x, bk.x, y);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (dm[k].x != 0.0f) o[k].x = S.x * dm[k].x / bk.x;
+        }
+    }
+    if (my) {
+        if (fy) {
+            const float y = __frcp_rn(bk.y);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) o[k].y = div_recip(S.y * dm[k].y, bk.y, y);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (dm[k].y != 0.0f) o[k].y = S.y * dm[k].y / bk.y;
+        }
+    }
+}
+
+// Layer 0 (rock) for two cells: drops b - nb[k] (nb is overwritten).
+__device__ __forceinline__ void cell_thermal_outflows2(const StepConsts& c, float2 b, float2 nb[8], float2 o[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) nb[k] = sub2(b, nb[k]);
+    cell_thermal_outflows_dh2(c.dt, c.Kalpha0, c.Kspeed0, c.talus_x_cross, c.talus_b_diag, c.fast_div, b, nb, o);
+}
+
+// backtrace + bilinear_mix for two cells at (x, y) and (x + 1, y): the
+// back-trace points and the mix weights on the pair, the clamps, floors and
+// tap indices per lane.
+__device__ __forceinline__ void backtrace2(const StepConsts& c, int x, int y, float2 u, float2 v, float2& px,
+                                           float2& py) {
+    const float maxc = (float)(c.n - 1);
+    const float2 tx = sub2(make_float2((float)x, (float)(x + 1)), mul2(u, pf(c.dt)));
+    const float2 ty = sub2(pf((float)y), mul2(v, pf(c.dt)));
+    px = make_float2(gclamp(tx.x, 0.0f, maxc), gclamp(tx.y, 0.0f, maxc));
+    py = make_float2(gclamp(ty.x, 0.0f, maxc), gclamp(ty.y, 0.0f, maxc));
+}
+__device__ __forceinline__ float2 gmix2(float2 x, float2 y, float2 a) {
+    return add2(mul2(x, sub2(pf(1.0f), a)), mul2(y, a));
+}
+__device__ __forceinline__ float2 bilinear_mix2(float2 px, float2 py, float2 s00, float2 s10, float2 s01,
+                                                float2 s11) {
+    const float2 fx = sub2(px, make_float2(floorf(px.x), floorf(px.y)));
+    const float2 fy = sub2(py, make_float2(floorf(py.x), floorf(py.y)));
+    return gmix2(gmix2(s00, s10, fx), gmix2(s01, s11, fx), fy);
+}
+
 // ---- thermal_transport (layer 0), glsl/thermal_transport.glsl:31-65 ----------------
 // own[k]: this cell's outflow in direction order L,R,T,B,LT,RT,LB,RB;
 // inflow: L.R, R.L, T.B, B.T, LT.RB, RT.LB, LB.RT, RB.LT (0 outside).

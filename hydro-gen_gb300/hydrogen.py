@@ -154,6 +154,7 @@ def _load():
         "hg_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_uint32, ctypes.POINTER(ctypes.c_int),
                                                     ctypes.POINTER(ctypes.c_double)]),
         "hg_selftest_report_timeout": (ctypes.c_int, [P]),
+        "hg_selftest_paired": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
         "hg_batch_launch_form": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
         "hg_batch_tuning": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_double)]),

@@ -490,6 +490,14 @@ int hg_selftest_division(uint64_t seed, uint64_t count, uint64_t* mismatches);
  * so 2^18 * ns_per_poll bounds a kernel's wait for a lost tile (about 1 s).  The device
  * stays usable afterwards.  Synchronises. */
 int hg_selftest_bounded_wait(uint32_t polls, int* timed_out, double* ns_per_poll);
+/* Device self-test of the paired (f32x2) arithmetic the kernels use, lane by
+ * lane against the scalar IEEE operations on `count` operand triples drawn
+ * from every float bit pattern (subnormals and zeros included):
+ * mismatches[0..4] count differing lanes of add, multiply, fused
+ * multiply-add, subtract and the shared-reciprocal quotient, mismatches[5]
+ * those of a product feeding a sum (which must round twice).  No
+ * counterpart in the reference. */
+int hg_selftest_paired(uint64_t seed, uint64_t count, uint64_t mismatches[6]);
 /* Test hook (no counterpart in the reference): sets the world's device error
  * flag from the host, as a kernel's bounded wait does when it gives up, so
  * that the HG_ERR_TIMEOUT contract of hg_sync can be tested without a GPU

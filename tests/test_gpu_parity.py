@@ -266,3 +266,13 @@ def test_shared_reciprocal_division_is_ieee_division():
     bad = ctypes.c_uint64()
     H.check(H.lib.hg_selftest_division(12345, 1 << 30, ctypes.byref(bad)))
     assert bad.value == 0
+
+
+def test_paired_arithmetic_is_scalar_arithmetic():
+    """The fused kernels evaluate two cells per f32x2 instruction; every lane
+    must round exactly as the scalar operation, subnormals included, and a
+    product feeding a sum must stay two roundings."""
+    import ctypes
+    bad = (ctypes.c_uint64 * 6)()
+    H.check(H.lib.hg_selftest_paired(777, 1 << 26, bad))
+    assert list(bad) == [0, 0, 0, 0, 0, 0], list(bad)
