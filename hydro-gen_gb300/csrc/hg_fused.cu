@@ -16,8 +16,7 @@
 //
 // Both kernels are table driven: one launch covers every tile of any number
 // of worlds ("terrains") of different sizes and settings.  A block finds its
-// terrain by binary search over the terrains' first tile (k_hydro) or first
-// block (k_transport) and reads the terrain's record (step constants, rain
+// terrain by binary search over the terrains' first tiles and reads the terrain's record (step constants, rain
 // settings, buffers, step counter; TMA tensor maps in global memory).  A
 // single world takes its whole descriptor, tensor maps included, as a kernel
 // parameter.  The rain step number comes from the terrain's device step
@@ -31,8 +30,11 @@
 //   iteration (low register use keeps ~6 blocks per SM to hide the long
 //   dependent chains of flux and erosion), a warp covering 32 consecutive
 //   cells of a row.
-//   k_transport: see its section below (talus warps sweeping a run of tiles
-//   with TMA double buffering, gather warps beside them).
+//   k_transport stages the eroded rock with a 2-row halo by one TMA load;
+//   each thread owns a row group of four horizontally adjacent cells: it
+//   computes their eight talus outflows once into shared memory (the ring of
+//   interior plus 1 too), applies outflow and inflow, and gathers the four
+//   sediment taps of every cell from L2/HBM.
 //
 // Per-cell arithmetic is the code of the per-pass kernels (hg_device.cuh),
 // evaluated two cells per f32x2 instruction where cells pair up, so the
@@ -59,10 +61,11 @@ constexpr int M_BERO = H_N;      // tensor map index of the eroded rock
 // Geometry of a 64 x TH tile: TH = 16 with 256 threads or TH = 8 with 128.
 template <int TH>
 struct Geo {
-    static constexpr int NTH = TH * GPR;                 // k_hydro: 4 cells per thread
+    static constexpr int NTH = TH * GPR;                 // one row group per thread in k_transport
     static constexpr int H_RH = TH + 2, H_BOX = RW * H_RH;
     static constexpr int H_RC = ((H_BOX + 31) / 32) * 32;  // 128-byte aligned array stride
     static constexpr int T_RH = TH + 4, T_BOX = RW * T_RH;
+    static constexpr int O_RH = TH + 2, O_C = RW * O_RH;   // outflows of interior plus 1
     static constexpr int CPT = TW * TH / NTH;             // cells per thread in k_hydro (4)
 };
 
@@ -231,84 +234,50 @@ __global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro1(const __grid_constant__
 }
 
 // ---------------------------------------------------------------------------
-// k_transport: sediment_transport and thermal_erosion/thermal_transport
-// (layer 0), one block per vertical run of SEG tiles of one 64-column strip,
-// with two kinds of warps:
-//
-//   talus warps sweep the run bottom to top.  The eroded rock of the next
-//   tile is on its way by TMA (two stage buffers, one mbarrier each) while a
-//   tile is computed.  Per tile they compute the talus outflows of the rows
-//   ty0 + 1 .. ty0 + TH (all 66 columns: the tile's and the two columns
-//   beside it) into shared memory, two cells per thread and f32x2 pair, and
-//   then apply every cell's own outflows and its eight neighbours'
-//   inflows.  Rows ty0 - 1 and ty0 were computed with the tile below and
-//   stay in shared memory, so each row's outflows are computed once per run
-//   instead of once per tile plus a two-row ring.  The work divides evenly:
-//   TH x 33 pairs over the talus threads.
-//
-//   gather warps do the semi-Lagrangian sediment gather of the run's cells
-//   from L2/HBM at their own pace (no barrier with the talus warps), so its
-//   load latency overlaps the talus arithmetic.
+// k_transport: sediment_transport, then thermal_erosion/thermal_transport
+// (layer 0).  The eroded rock of the 64 x TH tile and a two-row halo is
+// staged by one TMA load.  Each thread owns a row group of four cells,
+// evaluated as two f32x2 pairs: it issues the group's sediment taps before
+// the tile's TMA wait and mixes them after it, computes talus outflows (the
+// ring of interior plus one as pairs of ring cells, then its own group) into
+// shared memory, and after the block barrier applies its own outflows and
+// its neighbours' inflows.
 // ---------------------------------------------------------------------------
-template <int TH>
-struct TGeo {
-    static constexpr int TWP = TH == 16 ? 9 : 5;          // talus warps
-    static constexpr int GWP = TH == 16 ? 4 : 2;          // gather warps
-    static constexpr int TT = 32 * TWP;                   // talus threads
-    static constexpr int GT = 32 * GWP;                   // gather threads
-    static constexpr int NT = TT + GT;
-    static constexpr int OR = TH + 2;                     // outflow rows held: ty0 - 1 .. ty0 + TH
-    static constexpr int OPL = RW * OR;                   // outflow plane stride
-    static constexpr int PLANES = 9;                      // eight directions + the own-outflow sum
-    static constexpr int PPR = TW / 2 + 1;                // pairs per outflow row: 32 + the two side columns
-    static constexpr int SEG = 8;                         // tiles per block
-    static constexpr size_t SMEM = (2 * (size_t)Geo<TH>::T_BOX + PLANES * (size_t)OPL) * sizeof(float);
-};
 
-// Named barrier 1 over the talus warps only (the gather warps never join it).
-template <int TH>
-__device__ __forceinline__ void talus_sync() {
-    asm volatile("bar.sync 1, %0;" ::"r"(TGeo<TH>::TT) : "memory");
-}
-template <int TH>
-__device__ __forceinline__ bool talus_sync_and(bool p) {
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred pi, po;\n\t"
-        "setp.ne.u32 pi, %1, 0;\n\t"
-        "bar.red.and.pred po, 1, %2, pi;\n\t"
-        "selp.u32 %0, 1, 0, po;\n\t}"
-        : "=r"(r)
-        : "r"((uint32_t)p), "r"(TGeo<TH>::TT)
-        : "memory");
-    return r != 0;
+// Neighbour rock of the cell at region (rx, ry), global (gx, gy), in
+// direction order L, R, T, B, LT, RT, LB, RB (FAR_HEIGHT outside the grid).
+template <bool EDGE>
+__device__ __forceinline__ void talus_nb(const float* be, int rx, int ry, int gx, int gy, int n, float nb[8]) {
+    const int si = ry * RW + rx;
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {
+        bool out = false;
+        if (EDGE) {
+            const int xx = gx + f_ox[d], yy = gy + f_oy[d];
+            out = xx < 0 || xx >= n || yy < 0 || yy >= n;
+        }
+        nb[d] = out ? FAR_HEIGHT : be[si + f_oy[d] * RW + f_ox[d]];
+    }
 }
 
-// Talus outflows of a pair of cells from the staged eroded rock `be` (row 0
-// = global row gy0): lanes .x and .y at region (rxa, rya) and (rxb, ryb).
-// Neighbours outside the grid read FAR_HEIGHT; a cell outside the grid has
-// no outflows.
+// Talus outflows of two ring cells at once (lanes .x, .y) from the staged
+// eroded rock (row 0 = global row gy0, column 0 = global column gx0); a
+// cell outside the grid has none.
 template <bool EDGE>
 __device__ __forceinline__ void pair_outflows(const StepConsts& c, const float* be, int rxa, int rya, int rxb,
                                               int ryb, int gx0, int gy0, float2 o[8]) {
     const int n = c.n;
     const int gxa = gx0 + rxa, gya = gy0 + rya, gxb = gx0 + rxb, gyb = gy0 + ryb;
-    float2 nb[8];
+    const bool ina = !EDGE || (gxa >= 0 && gxa < n && gya >= 0 && gya < n);
+    const bool inb = !EDGE || (gxb >= 0 && gxb < n && gyb >= 0 && gyb < n);
+    float na[8], nbb[8];
+    talus_nb<EDGE>(be, rxa, rya, gxa, gya, n, na);
+    talus_nb<EDGE>(be, rxb, ryb, gxb, gyb, n, nbb);
+    float2 nb2[8];
 #pragma unroll
-    for (int d = 0; d < 8; ++d) {
-        float va = be[(rya + f_oy[d]) * RW + rxa + f_ox[d]];
-        float vb = be[(ryb + f_oy[d]) * RW + rxb + f_ox[d]];
-        if (EDGE) {
-            const int xa = gxa + f_ox[d], ya = gya + f_oy[d], xb = gxb + f_ox[d], yb = gyb + f_oy[d];
-            if (xa < 0 || xa >= n || ya < 0 || ya >= n) va = FAR_HEIGHT;
-            if (xb < 0 || xb >= n || yb < 0 || yb >= n) vb = FAR_HEIGHT;
-        }
-        nb[d] = make_float2(va, vb);
-    }
-    cell_thermal_outflows2(c, make_float2(be[rya * RW + rxa], be[ryb * RW + rxb]), nb, o);
+    for (int d = 0; d < 8; ++d) nb2[d] = make_float2(na[d], nbb[d]);
+    cell_thermal_outflows2(c, make_float2(be[rya * RW + rxa], be[ryb * RW + rxb]), nb2, o);
     if (EDGE) {
-        const bool ina = gxa >= 0 && gxa < n && gya >= 0 && gya < n;
-        const bool inb = gxb >= 0 && gxb < n && gyb >= 0 && gyb < n;
 #pragma unroll
         for (int d = 0; d < 8; ++d) {
             if (!ina) o[d].x = 0.0f;
@@ -317,213 +286,239 @@ __device__ __forceinline__ void pair_outflows(const StepConsts& c, const float* 
     }
 }
 
-// Outflow rows [r0, OR) of the tile at (tx0, ty0): outflow row lr is global
-// row ty0 - 1 + lr, eroded-rock row lr + 1.  Pair k < 32 of a row is the
-// cells tx0 + 2k, tx0 + 2k + 1; pair 32 the two side columns tx0 - 1 and
-// tx0 + 64.  Each pair's eight outflows and the sums 0 - o[0] - ... - o[7]
-// go to the planes.
-template <int TH, bool EDGE>
-__device__ __forceinline__ void talus_rows(const StepConsts& c, const float* be, float* outf, int tx0, int ty0,
-                                           int r0, int tt) {
-    using T = TGeo<TH>;
-    const int npairs = (T::OR - r0) * T::PPR;
-    const int gx0 = tx0 - HX, gy0 = ty0 - 2;
-    for (int p = tt; p < npairs; p += T::TT) {
-        const int lr = r0 + p / T::PPR, k = p % T::PPR;
-        const bool side = k == T::PPR - 1;
-        const int rxa = side ? HX - 1 : HX + 2 * k, rxb = side ? HX + TW : rxa + 1;
-        float2 o[8];
-        pair_outflows<EDGE>(c, be, rxa, lr + 1, rxb, lr + 1, gx0, gy0, o);
-        float2 sum = pf(0.0f);
+// Talus outflows of the row group of four cells at region (rx0, ry), global
+// (x0, y), as two pairs (cells 0, 1 and 2, 3), stored to outf (direction
+// stride o_c, the group's first cell at oi); osum[h] receives pair h's
+// 0 - own[0] - ... - own[7].  A row outside the grid has none.
+template <bool EDGE>
+__device__ __forceinline__ void group_outflows(const StepConsts& c, const float* be, int rx0, int ry, int x0, int y,
+                                               float* outf, int o_c, int oi, float2 osum[2]) {
+    const int n = c.n;
+    osum[0] = osum[1] = pf(0.0f);
+    if (EDGE && (y < 0 || y >= n)) {
 #pragma unroll
-        for (int d = 0; d < 8; ++d) sum = sub2(sum, o[d]);
-        const int oa = lr * RW + rxa, ob = lr * RW + rxb;
-        if (!side) {  // adjacent and 8-byte aligned
+        for (int d = 0; d < 8; ++d) st4(outf + d * o_c + oi, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        return;
+    }
+    const int si = ry * RW + rx0;
+    const float4 m4 = ld4(be + si - RW), c4 = ld4(be + si), p4 = ld4(be + si + RW);
+    const float ml = be[si - RW - 1], mr = be[si - RW + 4];
+    const float cl = be[si - 1], cr = be[si + 4];
+    const float pl = be[si + RW - 1], pr = be[si + RW + 4];
+    float nb[4][8];
 #pragma unroll
-            for (int d = 0; d < 8; ++d) *reinterpret_cast<float2*>(outf + d * T::OPL + oa) = o[d];
-            *reinterpret_cast<float2*>(outf + 8 * T::OPL + oa) = sum;
-        } else {
+    for (int j = 0; j < 4; ++j) {
+        const int x = x0 + j;
+        const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
+        const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
+        nb[j][0] = has_l ? (j == 0 ? cl : at4(c4, j - 1)) : FAR_HEIGHT;
+        nb[j][1] = has_r ? (j == 3 ? cr : at4(c4, j + 1)) : FAR_HEIGHT;
+        nb[j][2] = has_t ? at4(p4, j) : FAR_HEIGHT;
+        nb[j][3] = has_b ? at4(m4, j) : FAR_HEIGHT;
+        nb[j][4] = (has_l && has_t) ? (j == 0 ? pl : at4(p4, j - 1)) : FAR_HEIGHT;
+        nb[j][5] = (has_r && has_t) ? (j == 3 ? pr : at4(p4, j + 1)) : FAR_HEIGHT;
+        nb[j][6] = (has_l && has_b) ? (j == 0 ? ml : at4(m4, j - 1)) : FAR_HEIGHT;
+        nb[j][7] = (has_r && has_b) ? (j == 3 ? mr : at4(m4, j + 1)) : FAR_HEIGHT;
+    }
 #pragma unroll
-            for (int d = 0; d < 8; ++d) {
-                outf[d * T::OPL + oa] = o[d].x;
-                outf[d * T::OPL + ob] = o[d].y;
-            }
-            outf[8 * T::OPL + oa] = sum.x;
-            outf[8 * T::OPL + ob] = sum.y;
+    for (int h = 0; h < 2; ++h) {
+        float2 nb2[8], o[8];
+#pragma unroll
+        for (int d = 0; d < 8; ++d) nb2[d] = make_float2(nb[2 * h][d], nb[2 * h + 1][d]);
+        cell_thermal_outflows2(c, make_float2(at4(c4, 2 * h), at4(c4, 2 * h + 1)), nb2, o);
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            osum[h] = sub2(osum[h], o[d]);
+            *reinterpret_cast<float2*>(outf + d * o_c + oi + 2 * h) = o[d];
         }
     }
 }
 
-// thermal_transport of the tile's row groups (four cells each): rock = b +
-// (own sum + in_flux), in_flux = in[0] + ... + in[7] from 0 in the order L.R,
-// R.L, T.B, B.T, LT.RB, RT.LB, LB.RT, RB.LT (cell_thermal_apply's operations).
-template <int TH>
-__device__ __forceinline__ void talus_apply(const TerrainHot& td, const float* be, const float* outf, int tx0,
-                                            int ty0, int tt) {
-    using T = TGeo<TH>;
-    const int n = td.c.n;
-    for (int q = tt; q < TH * GPR; q += T::TT) {
-        const int iy = q / GPR, g = q % GPR;
-        const int rx0 = HX + 4 * g;
-        const int oi = (iy + 1) * RW + rx0;  // outflow row of global row ty0 + iy
+template <int TH, bool EDGE>
+__device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUtensorMap* maps, float* be, float* outf,
+                                               uint64_t* bar, int tx0, int ty0, int* err) {
+    using G = Geo<TH>;
+    constexpr int O_C = G::O_C;
+    const StepConsts& c = td.c;
+    const int n = c.n;
+    const int tid = threadIdx.x;
+    const int gx0 = tx0 - HX, gy0 = ty0 - 2;
+    if (c.thermal && tid == 0) {
+        mbar_arrive_expect_tx(bar, G::T_BOX * sizeof(float));
+        tma_load_2d(be, &maps[M_BERO], gx0, gy0, bar);
+    }
+    const int iy = tid / GPR, g = tid % GPR;
+    const int x0 = tx0 + 4 * g, y = ty0 + iy;
+    const size_t gi0 = (size_t)y * n + x0;
+    const float4 u4 = __ldg(reinterpret_cast<const float4*>(td.u + gi0));
+    const float4 v4 = __ldg(reinterpret_cast<const float4*>(td.v + gi0));
+
+    // sediment_transport: semi-Lagrangian gather of eroded sediment (any
+    // reach), two cells per pair.  The taps' loads stay in flight across the
+    // tile's TMA wait.
+    float2 bx[2], by[2], t00[2], t10[2], t01[2], t11[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        backtrace2(c, x0 + 2 * h, y, make_float2(at4(u4, 2 * h), at4(u4, 2 * h + 1)),
+                   make_float2(at4(v4, 2 * h), at4(v4, 2 * h + 1)), bx[h], by[h]);
+        float tap[4][2];
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            const float px = l ? bx[h].y : bx[h].x, py = l ? by[h].y : by[h].x;
+            const int ix = min(max((int)px, 0), n - 1), iy2 = min(max((int)py, 0), n - 1);
+            const float* se = td.s_ero + (size_t)iy2 * n + ix;
+            tap[0][l] = __ldg(se);
+            tap[1][l] = ix + 1 < n ? __ldg(se + 1) : 0.0f;
+            tap[2][l] = iy2 + 1 < n ? __ldg(se + n) : 0.0f;
+            tap[3][l] = (ix + 1 < n && iy2 + 1 < n) ? __ldg(se + n + 1) : 0.0f;
+        }
+        t00[h] = make_float2(tap[0][0], tap[0][1]);
+        t10[h] = make_float2(tap[1][0], tap[1][1]);
+        t01[h] = make_float2(tap[2][0], tap[2][1]);
+        t11[h] = make_float2(tap[3][0], tap[3][1]);
+    }
+    auto finish_sed = [&]() {
+        const float2 s0 = bilinear_mix2(bx[0], by[0], t00[0], t10[0], t01[0], t11[0]);
+        const float2 s1 = bilinear_mix2(bx[1], by[1], t00[1], t10[1], t01[1], t11[1]);
+        st4(td.out[S_SED] + gi0, make_float4(s0.x, s0.y, s1.x, s1.y));
+    };
+    if (!c.thermal) {
+        finish_sed();
+        return;
+    }
+
+    bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+        mbar_wait(bar, 0);
+        return;
+    }
+    // the taps' loads were issued with the tile's copy: mix them now, before
+    // the outflows need the registers
+    finish_sed();
+    // ---- outflows of the ring of interior plus 1, two cells per thread -----
+    // pairs: 32 on the top ring row, 32 on the bottom one, then the left and
+    // right ring columns row by row
+    {
+        constexpr int RINGP = TW + TH + 2;
+        for (int q = tid; q < RINGP; q += G::NTH) {
+            int rxa, rya, rxb, ryb;
+            if (q < TW / 2) { rxa = HX + 2 * q; rya = 1; rxb = rxa + 1; ryb = 1; }
+            else if (q < TW) { rxa = HX + 2 * (q - TW / 2); rya = TH + 2; rxb = rxa + 1; ryb = TH + 2; }
+            else { rxa = HX - 1; rya = 1 + q - TW; rxb = HX + TW; ryb = rya; }
+            float2 o2[8];
+            pair_outflows<EDGE>(c, be, rxa, rya, rxb, ryb, gx0, gy0, o2);
+            const int roa = (rya - 1) * RW + rxa, rob = (ryb - 1) * RW + rxb;
+            if (q < TW) {  // horizontally adjacent: one 8-byte store per direction
+#pragma unroll
+                for (int d = 0; d < 8; ++d) *reinterpret_cast<float2*>(outf + d * O_C + roa) = o2[d];
+            } else {
+#pragma unroll
+                for (int d = 0; d < 8; ++d) {
+                    outf[d * O_C + roa] = o2[d].x;
+                    outf[d * O_C + rob] = o2[d].y;
+                }
+            }
+        }
+    }
+    // ---- outflows of the interior row groups (one per thread) --------------
+    // The thread's own outflow sums (cell_thermal_apply's sum = 0 - own[0] -
+    // ... - own[7]) stay in registers.
+    const int rx0 = HX + 4 * g, ry = 2 + iy;  // region coords of the group's first cell
+    const int oi = (ry - 1) * RW + rx0;
+    float2 osum[2];
+    group_outflows<EDGE>(c, be, rx0, ry, x0, y, outf, O_C, oi, osum);
+    __syncthreads();
+    // ---- thermal_transport: own outflows out, neighbours' outflows in -------
+    // (cell_thermal_apply's operations: in_flux = in[0] + ... + in[7] from 0,
+    // sum = 0 - own[0] - ... - own[7], rock = b + (sum + in_flux))
+    {
+        // inflow from direction d = neighbour (dx, dy)'s outflow toward this
+        // cell.  Rows of outflows are read as aligned float4 (the group's own
+        // four columns); the column left (right) of the group comes from the
+        // neighbouring group in the warp, lane - 1 (+ 1), or at the tile edge
+        // from the ring column.
+        const unsigned FULL = 0xffffffffu;
+        const bool first = g == 0, last = g == GPR - 1;
         // left neighbour's direction-dl outflow and right neighbour's
-        // direction-dr outflow, row at offset `off`, for the four cells
+        // direction-dr outflow in the row at offset `off`, as cell pairs
         auto row_in = [&](int dl, int dr, int off, float2 in[2][2]) {
-            const float4 a = ld4(outf + dl * T::OPL + oi + off), b = ld4(outf + dr * T::OPL + oi + off);
-            const float pa = outf[dl * T::OPL + oi + off - 1], nb = outf[dr * T::OPL + oi + off + 4];
+            const float4 a = ld4(outf + dl * O_C + oi + off), b = ld4(outf + dr * O_C + oi + off);
+            float pa = __shfl_up_sync(FULL, a.w, 1);
+            float nb = __shfl_down_sync(FULL, b.x, 1);
+            if (first) pa = outf[dl * O_C + oi + off - 1];
+            if (last) nb = outf[dr * O_C + oi + off + 4];
             in[0][0] = make_float2(pa, a.x);
             in[0][1] = make_float2(a.y, a.z);
             in[1][0] = make_float2(b.y, b.z);
             in[1][1] = make_float2(b.w, nb);
         };
         float2 inf[2] = {pf(0.0f), pf(0.0f)};
+        auto acc = [&](const float2 v[2]) {
+            inf[0] = add2(inf[0], v[0]);
+            inf[1] = add2(inf[1], v[1]);
+        };
         {
             float2 in[2][2];
             row_in(1, 0, 0, in);  // L neighbour's R, R neighbour's L
-            inf[0] = add2(inf[0], in[0][0]); inf[1] = add2(inf[1], in[0][1]);
-            inf[0] = add2(inf[0], in[1][0]); inf[1] = add2(inf[1], in[1][1]);
+            acc(in[0]);
+            acc(in[1]);
         }
         {
-            const float4 inT = ld4(outf + 3 * T::OPL + oi + RW);  // top neighbour's B
-            const float4 inB = ld4(outf + 2 * T::OPL + oi - RW);  // bottom neighbour's T
-            inf[0] = add2(inf[0], make_float2(inT.x, inT.y)); inf[1] = add2(inf[1], make_float2(inT.z, inT.w));
-            inf[0] = add2(inf[0], make_float2(inB.x, inB.y)); inf[1] = add2(inf[1], make_float2(inB.z, inB.w));
+            const float4 inT = ld4(outf + 3 * O_C + oi + RW);  // top neighbour's B
+            const float4 inB = ld4(outf + 2 * O_C + oi - RW);  // bottom neighbour's T
+            const float2 t[2] = {make_float2(inT.x, inT.y), make_float2(inT.z, inT.w)};
+            const float2 bb[2] = {make_float2(inB.x, inB.y), make_float2(inB.z, inB.w)};
+            acc(t);
+            acc(bb);
         }
         {
             float2 in[2][2];
             row_in(7, 6, RW, in);  // row above: LT neighbour's RB, RT neighbour's LB
-            inf[0] = add2(inf[0], in[0][0]); inf[1] = add2(inf[1], in[0][1]);
-            inf[0] = add2(inf[0], in[1][0]); inf[1] = add2(inf[1], in[1][1]);
+            acc(in[0]);
+            acc(in[1]);
         }
         {
             float2 in[2][2];
             row_in(5, 4, -RW, in);  // row below: LB neighbour's RT, RB neighbour's LT
-            inf[0] = add2(inf[0], in[0][0]); inf[1] = add2(inf[1], in[0][1]);
-            inf[0] = add2(inf[0], in[1][0]); inf[1] = add2(inf[1], in[1][1]);
+            acc(in[0]);
+            acc(in[1]);
         }
-        const float4 own = ld4(outf + 8 * T::OPL + oi);
-        const float4 b4 = ld4(be + (iy + 2) * RW + rx0);
-        const float2 r0 = add2(make_float2(b4.x, b4.y), add2(make_float2(own.x, own.y), inf[0]));
-        const float2 r1 = add2(make_float2(b4.z, b4.w), add2(make_float2(own.z, own.w), inf[1]));
-        const size_t gi0 = (size_t)(ty0 + iy) * n + tx0 + 4 * g;
+        const float4 b4 = ld4(be + ry * RW + rx0);
+        const float2 r0 = add2(make_float2(b4.x, b4.y), add2(osum[0], inf[0]));
+        const float2 r1 = add2(make_float2(b4.z, b4.w), add2(osum[1], inf[1]));
         st4(td.out[S_ROCK] + gi0, make_float4(r0.x, r0.y, r1.x, r1.y));
     }
 }
 
-// The semi-Lagrangian gather of the row group of four cells at (x0, y), as
-// two pairs (glsl/sediment_transport.glsl:70-72, img_interpolation.glsl:3-22).
-__device__ __forceinline__ void gather_group(const TerrainHot& td, int x0, int y) {
-    const StepConsts& c = td.c;
-    const int n = c.n;
-    const size_t gi0 = (size_t)y * n + x0;
-    const float4 u4 = __ldg(reinterpret_cast<const float4*>(td.u + gi0));
-    const float4 v4 = __ldg(reinterpret_cast<const float4*>(td.v + gi0));
-    float2 sed[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float2 bx, by;
-        backtrace2(c, x0 + 2 * h, y, make_float2(at4(u4, 2 * h), at4(u4, 2 * h + 1)),
-                   make_float2(at4(v4, 2 * h), at4(v4, 2 * h + 1)), bx, by);
-        float tap[4][2];
-#pragma unroll
-        for (int l = 0; l < 2; ++l) {
-            const float px = l ? bx.y : bx.x, py = l ? by.y : by.x;
-            const int ix = min(max((int)px, 0), n - 1), iy = min(max((int)py, 0), n - 1);
-            const float* se = td.s_ero + (size_t)iy * n + ix;
-            tap[0][l] = __ldg(se);
-            tap[1][l] = ix + 1 < n ? __ldg(se + 1) : 0.0f;
-            tap[2][l] = iy + 1 < n ? __ldg(se + n) : 0.0f;
-            tap[3][l] = (ix + 1 < n && iy + 1 < n) ? __ldg(se + n + 1) : 0.0f;
-        }
-        sed[h] = bilinear_mix2(bx, by, make_float2(tap[0][0], tap[0][1]), make_float2(tap[1][0], tap[1][1]),
-                               make_float2(tap[2][0], tap[2][1]), make_float2(tap[3][0], tap[3][1]));
-    }
-    st4(td.out[S_SED] + gi0, make_float4(sed[0].x, sed[0].y, sed[1].x, sed[1].y));
-}
-
-// One block: the run of tiles k0 .. k1 - 1 (rows of tiles) of strip sx of a
-// terrain; `blk` is the block's index within the terrain.
 template <int TH>
-__device__ __forceinline__ void transport_run(const TerrainHot& td, const CUtensorMap* maps, int blk, int* err) {
-    using T = TGeo<TH>;
-    extern __shared__ __align__(128) float tr_sm[];
-    float* be[2] = {tr_sm, tr_sm + Geo<TH>::T_BOX};
-    float* outf = tr_sm + 2 * Geo<TH>::T_BOX;
-    __shared__ __align__(8) uint64_t bar[2];
-    const StepConsts& c = td.c;
-    const int n = c.n;
-    const int tiles_y = n / TH;
-    const int sx = blk % td.tiles_x, seg = blk / td.tiles_x;
-    const int k0 = seg * T::SEG, k1 = min(k0 + T::SEG, tiles_y);
-    const int tx0 = sx * TW;
-    const int tid = threadIdx.x;
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-    }
+__device__ __forceinline__ void transport_block(const TerrainHot& td, const CUtensorMap* maps, int tile, int* err) {
+    using G = Geo<TH>;
+    __shared__ __align__(128) float be[G::T_BOX];
+    __shared__ __align__(16) float outf[8 * G::O_C];
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
-    if (tid >= T::TT) {  // ---- gather warps ----
-        const int gt = tid - T::TT;
-        for (int k = k0; k < k1; ++k)
-            for (int q = gt; q < TH * GPR; q += T::GT) gather_group(td, tx0 + 4 * (q % GPR), k * TH + q / GPR);
-        // k_hydro of this step has finished (stream order) and the next
-        // step's k_hydro starts after this launch: advance the step counter
-        if (blk == 0 && gt == 0) *td.step += 1ull;
-        return;
-    }
-    if (!c.thermal) return;
-    // ---- talus warps ----
-    const int tt = tid;
-    auto issue = [&](int k, int stage) {  // thread 0: the eroded rock box of tile row k
-        // the buffer's previous contents were read by every talus thread
-        // (ordered by the barrier before this call); order those reads
-        // before the async-proxy write
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive_expect_tx(&bar[stage], Geo<TH>::T_BOX * sizeof(float));
-        tma_load_2d(be[stage], &maps[M_BERO], tx0 - HX, k * TH - 2, &bar[stage]);
-    };
-    if (tt == 0) issue(k0, 0);
-    uint32_t parity = 0;  // bit s: parity of stage s's next completion
-    for (int k = k0; k < k1; ++k) {
-        const int stage = (k - k0) & 1;
-        const bool ok = talus_sync_and<TH>(mbar_wait(&bar[stage], (parity >> stage) & 1u));
-        if (!ok) {  // the tile never arrived: record, give the copy one more bounded wait, stop
-            if (tt == 0) atomicExch(err, 1);
-            mbar_wait(&bar[stage], (parity >> stage) & 1u);
-            return;
-        }
-        parity ^= 1u << stage;
-        if (tt == 0 && k + 1 < k1) issue(k + 1, stage ^ 1);
-        const int ty0 = k * TH;
-        const bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 2 >= 0 && ty0 + TH + 2 <= n;
-        const int r0 = k == k0 ? 0 : 2;
-        if (inner) talus_rows<TH, false>(c, be[stage], outf, tx0, ty0, r0, tt);
-        else talus_rows<TH, true>(c, be[stage], outf, tx0, ty0, r0, tt);
-        talus_sync<TH>();
-        talus_apply<TH>(td, be[stage], outf, tx0, ty0, tt);
-        if (k + 1 < k1) {
-            talus_sync<TH>();  // every apply has read the outflows
-            // rows ty0 + TH - 1 and ty0 + TH become the next tile's rows 0, 1
-            for (int i = tt; i < T::PLANES * 2 * RW; i += T::TT) {
-                const int pl = i / (2 * RW), r = i % (2 * RW);
-                outf[pl * T::OPL + r] = outf[pl * T::OPL + (T::OR - 2) * RW + r];
-            }
-        }
-    }
+    const int n = td.c.n;
+    const int tx0 = (tile % td.tiles_x) * TW, ty0 = (tile / td.tiles_x) * TH;
+    bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 2 >= 0 && ty0 + TH + 2 <= n;
+    if (inner) transport_tile<TH, false>(td, maps, be, outf, &bar, tx0, ty0, err);
+    else transport_tile<TH, true>(td, maps, be, outf, &bar, tx0, ty0, err);
+    // k_hydro of this step has finished (stream order) and the next step's
+    // k_hydro starts after this launch: advance the terrain's step counter
+    if (tile == 0 && threadIdx.x == 0) *td.step += 1ull;
 }
 
 template <int TH>
-__global__ void __launch_bounds__(TGeo<TH>::NT, TH == 16 ? 2 : 4) k_transport(const __grid_constant__ BatchParams bp,
-                                                                       const CUtensorMap* __restrict__ maps,
-                                                                       int* err) {
-    const int t = find_terrain(bp.blk0, bp.nterr, blockIdx.x);
-    transport_run<TH>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.blk0[t], err);
+__global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport(const __grid_constant__ BatchParams bp,
+                                                            const CUtensorMap* __restrict__ maps, int* err) {
+    const int t = find_terrain(bp.tile0, bp.nterr, blockIdx.x);
+    transport_block<TH>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
 }
 
 template <int TH>
-__global__ void __launch_bounds__(TGeo<TH>::NT, TH == 16 ? 2 : 4) k_transport1(const __grid_constant__ TerrainDesc td,
-                                                                        int* err) {
-    transport_run<TH>(td.h, td.maps, blockIdx.x, err);
+__global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport1(const __grid_constant__ TerrainDesc td, int* err) {
+    transport_block<TH>(td.h, td.maps, blockIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -589,48 +584,28 @@ bool fill_desc(TerrainDesc& d, const TerrainSrc& s, int th, int tile0, TmaCache&
     return cache.get(s.b_ero, s.c.n, th + 4, &d.maps[M_BERO]);
 }
 
-int sweep_blocks(int n, int th) {
-    const int seg = th == 16 ? TGeo<16>::SEG : TGeo<8>::SEG;
-    return (n / TW) * ((n / th + seg - 1) / seg);
-}
-
-namespace {
-template <int TH, class K>
-void set_transport_smem(K kernel) {
-    static std::once_flag once;
-    std::call_once(once, [&] {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TGeo<TH>::SMEM);
-    });
-}
-
-template <int TH>
-void launch_table(const BatchParams& bp, const CUtensorMap* maps, int total_tiles, int* err, cudaStream_t st) {
-    int blocks = 0;
-    for (int i = 0; i < bp.nterr; ++i) blocks += sweep_blocks(bp.t[i].c.n, TH);
-    set_transport_smem<TH>(k_transport<TH>);
-    k_hydro<TH><<<total_tiles, Geo<TH>::NTH, 0, st>>>(bp, maps, err);
-    k_transport<TH><<<blocks, TGeo<TH>::NT, TGeo<TH>::SMEM, st>>>(bp, maps, err);
-    count_launch(2);
-}
-
-template <int TH>
-void launch_one(const TerrainDesc& td, int* err, cudaStream_t st) {
-    set_transport_smem<TH>(k_transport1<TH>);
-    k_hydro1<TH><<<fused_tiles(td.h.c.n, TH), Geo<TH>::NTH, 0, st>>>(td, err);
-    k_transport1<TH><<<sweep_blocks(td.h.c.n, TH), TGeo<TH>::NT, TGeo<TH>::SMEM, st>>>(td, err);
-    count_launch(2);
-}
-}  // namespace
-
 void launch_fused_table(const BatchParams& bp, const CUtensorMap* maps, int total_tiles, int th, int* err,
                         cudaStream_t st) {
-    if (th == 16) launch_table<16>(bp, maps, total_tiles, err, st);
-    else launch_table<8>(bp, maps, total_tiles, err, st);
+    if (th == 16) {
+        k_hydro<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(bp, maps, err);
+        k_transport<16><<<total_tiles, Geo<16>::NTH, 0, st>>>(bp, maps, err);
+    } else {
+        k_hydro<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(bp, maps, err);
+        k_transport<8><<<total_tiles, Geo<8>::NTH, 0, st>>>(bp, maps, err);
+    }
+    count_launch(2);
 }
 
 void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st) {
-    if (th == 16) launch_one<16>(td, err, st);
-    else launch_one<8>(td, err, st);
+    const int tiles = fused_tiles(td.h.c.n, th);
+    if (th == 16) {
+        k_hydro1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);
+        k_transport1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);
+    } else {
+        k_hydro1<8><<<tiles, Geo<8>::NTH, 0, st>>>(td, err);
+        k_transport1<8><<<tiles, Geo<8>::NTH, 0, st>>>(td, err);
+    }
+    count_launch(2);
 }
 
 }  // namespace hg

@@ -175,7 +175,6 @@ constexpr int MAX_BATCH = 128;
 struct BatchParams {
     int nterr;
     int tile0[MAX_BATCH];
-    int blk0[MAX_BATCH];  // first block of each terrain in a transport launch
     TerrainHot t[MAX_BATCH];
 };
 static_assert(sizeof(BatchParams) < 32000, "kernel parameter space");
@@ -207,8 +206,6 @@ struct TmaCache {
 // Tile height th (16 or 8) divides n and 64 divides n.
 bool fused_tile_ok(int n, int th);
 int fused_tiles(int n, int th);
-// Blocks of one terrain in a transport launch (runs of tile rows per strip).
-int sweep_blocks(int n, int th);
 // Fills a descriptor (tensor maps from the cache); false if a map cannot be encoded.
 bool fill_desc(TerrainDesc& d, const TerrainSrc& s, int th, int tile0, TmaCache& cache);
 // k_hydro then k_transport over every tile of the batch's terrains; maps

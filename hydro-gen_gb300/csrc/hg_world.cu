@@ -459,11 +459,8 @@ int build_plan(Plan* p) {
             BatchParams& bp = *p->bp[dir];
             bp.nterr = (int)nt;
             std::vector<CUtensorMap> maps(nt * MAPS_PER_TERRAIN);
-            int blk = 0;
             for (size_t i = 0; i < nt; ++i) {
                 bp.tile0[i] = tile0[i];
-                bp.blk0[i] = blk;
-                blk += sweep_blocks(p->worlds[i]->n, p->th);
                 bp.t[i] = tab[i].h;
                 for (int m = 0; m < MAPS_PER_TERRAIN; ++m) maps[i * MAPS_PER_TERRAIN + m] = tab[i].maps[m];
             }
