@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
     ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint", "adjoint_thermal",
-                                        "batch", "config1", "fp64_error", "fit_study"],
+                                        "batch", "config1", "fp64_error", "fit_study", "large", "fd_check"],
                     default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
@@ -161,16 +161,22 @@ def cpu_baseline(n_sample=1024, budget_s=12.0):
                       f"(float oracle, OpenMP over rows)"}
 
 
-def fd_check(H, torch, w, tape, reset, b0, target, n, nsteps, g, dks, db0, cells=64, eps=1e-3, seed=0):
+def fd_check(H, torch, w, tape, reset, b0, target, n, nsteps, g, dks, db0, cells=64, eps=(1e-3, 1e-5), seed=0,
+             reference_adjoint=False):
     """The GPU adjoint's gradients at the fit's starting point (uniform Ks
     0.05, the initial rock) against central finite differences of the FP64
-    reference forward (eps 1e-3) on `cells` random cells (fixed seed), for
-    both the per-cell Ks and the initial rock.  The FP64 differences run on
-    all host cores (each perturbed forward only where it differs from an
-    unperturbed one run in lockstep, bit for bit the full forward).
-    Relative error |g - fd| / max(|fd|, 1e-2 max|g|): the floor keeps cells
-    whose gradient is ~0 (deposition, where Ks has no effect) from dividing
-    by noise."""
+    reference forward on `cells` random cells (fixed seed), for both the
+    per-cell Ks and the initial rock, at each step size in `eps`.  The FP64
+    differences run on all host cores (each perturbed forward only where it
+    differs from an unperturbed one run in lockstep, bit for bit the full
+    forward).  Relative error |g - fd| / max(|fd|, 1e-2 max|g|): the floor
+    keeps cells whose gradient is ~0 (deposition, where Ks has no effect)
+    from dividing by noise.  The scheme is piecewise smooth (dissolve or
+    deposit, clamps, maxima), and over 256 steps a difference of 1e-3
+    straddles a switch at a share of the cells, so 1e-5 is reported beside
+    it.  With reference_adjoint the FP64 reference adjoint of the same loss
+    (minutes of host time) is compared too: with the FD and with the GPU
+    over every cell."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     ks = np.full((n, n), 0.05, np.float32)
@@ -181,24 +187,40 @@ def fd_check(H, torch, w, tape, reset, b0, target, n, nsteps, g, dks, db0, cells
     tape.backward(g.data_ptr(), dks.data_ptr(), db0.data_ptr())
     w.sync()
     gk, gb = dks.cpu().numpy().astype(np.float64), db0.cpu().numpy().astype(np.float64)
+    tgt = target.cpu().numpy().astype(np.float64)
     rng = np.random.default_rng(seed)
     pick = rng.choice(n * n, size=cells, replace=False)
-    t0 = time.perf_counter()
-    fd = O.fd_ref(O.settings_config1(), 0.01, 1, b0.astype(np.float64), ks, target.cpu().numpy().astype(np.float64),
-                  nsteps, np.concatenate([pick, pick]), np.array([0] * cells + [1] * cells), eps)
-    el = time.perf_counter() - t0
-    out = {"cells": cells, "eps": eps, "seed": seed, "loss": loss, "fd_seconds": el, "fd_cores": O.num_threads(),
-           "tolerance": 1e-3, "relative_error": "|g - fd| / max(|fd|, 1e-2 max|g|)"}
-    for name, grad, fdv in (("ks", gk, fd[:cells]), ("rock0", gb, fd[cells:])):
+    out = {"cells": cells, "seed": seed, "loss": loss, "fd_cores": O.num_threads(), "tolerance": 1e-3,
+           "relative_error": "|g - fd| / max(|fd|, 1e-2 max|g|)"}
+
+    def compare(grad, fdv):
         gv = grad.flat[pick]
         rel = np.abs(gv - fdv) / np.maximum(np.abs(fdv), 1e-2 * np.abs(grad).max())
-        out[name] = {"within_tol": int(np.sum(rel <= 1e-3)), "max_rel": float(rel.max()),
-                     "median_rel": float(np.median(rel)), "max_abs_grad": float(np.abs(grad).max())}
+        return {"within_tol": int(np.sum(rel <= 1e-3)), "max_rel": float(rel.max()),
+                "median_rel": float(np.median(rel))}
+
+    fds = {}
+    for e in eps:
+        t0 = time.perf_counter()
+        fd = O.fd_ref(O.settings_config1(), 0.01, 1, b0.astype(np.float64), ks, tgt, nsteps,
+                      np.concatenate([pick, pick]), np.array([0] * cells + [1] * cells), e)
+        fds[e] = fd
+        out[f"eps_{e:g}"] = {"fd_seconds": time.perf_counter() - t0, "gpu_ks": compare(gk, fd[:cells]),
+                             "gpu_rock0": compare(gb, fd[cells:])}
+    if reference_adjoint:
+        t0 = time.perf_counter()
+        _, rk, rb = O.adjoint_ref(O.settings_config1(), 0.01, 1, b0.astype(np.float64), ks, tgt, nsteps)
+        out["reference_adjoint_seconds"] = time.perf_counter() - t0
+        for e, fd in fds.items():
+            out[f"eps_{e:g}"]["fp64_adjoint_ks"] = compare(rk, fd[:cells])
+            out[f"eps_{e:g}"]["fp64_adjoint_rock0"] = compare(rb, fd[cells:])
+        out["gpu_vs_fp64_adjoint_rel_l2"] = {"ks": float(np.linalg.norm(gk - rk) / np.linalg.norm(rk)),
+                                             "rock0": float(np.linalg.norm(gb - rb) / np.linalg.norm(rb))}
     w.sync()
     return out
 
 
-def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fd_cells=64, fit_kw=None):
+def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fd_cells=64, fit_kw=None, reference_adjoint=False):
     """Forward + adjoint of the inverse-erosion workload: 1024^2, config-1
     physics, per-cell Ks = 0.05 exp(0.5 n(x)) from 3-octave simplex noise,
     MSE to a target, gradients for Ks and the initial rock; then fit_iters
@@ -241,7 +263,8 @@ def bench_adjoint(H, torch, n=1024, nsteps=256, ckpt=32, reps=3, fd_cells=64, fi
             all_ms.append(e0.elapsed_time(e2))
     f, a = statistics.median(fwd_ms), statistics.median(all_ms)
     cs = n * n * nsteps
-    fd = fd_check(H, torch, w, tape, reset, b0, target, n, nsteps, g, dks, db0) if fd_cells else None
+    fd = (fd_check(H, torch, w, tape, reset, b0, target, n, nsteps, g, dks, db0, cells=fd_cells,
+                   reference_adjoint=reference_adjoint) if fd_cells else None)
     # the fit itself (hg_inverse_fit) from uniform Ks = 0.05 and the true
     # initial rock
     fit = bench_fit(H, torch, w, target, ks_true, b0, n, nsteps, ckpt, **(fit_kw or {}))
@@ -301,12 +324,12 @@ def bench_fit(H, torch, w, target, ks_true, b0, n, nsteps, ckpt, iters=100, chun
             "loss_first": losses[0], "loss_last": losses[-1]}
 
 
-def bench_adjoint_workload(H, torch, n=N_GRID, nsteps=100, reps=2):
+def bench_adjoint_workload(H, torch, n=N_GRID, nsteps=500, reps=2):
     """Forward + adjoint at the metric's workload (4096^2, Bernoulli rain,
-    talus slippage) with a per-cell Ks field: nsteps taped steps from the
-    initial heightmap, checkpoint interval chosen from free memory (the whole
-    tape fits here, so nothing is recomputed), MSE to a target, gradients for
-    Ks and the initial rock."""
+    talus slippage, its 500 steps) with a per-cell Ks field: nsteps taped
+    steps from the initial heightmap, checkpoint interval chosen from free
+    memory (the steps beyond one segment are recomputed in the backward),
+    MSE to a target, gradients for Ks and the initial rock."""
     w = H.World(n)
     w.init_heightmap(H.noise(seed=0))
     H.configure(w, "config2")
@@ -338,7 +361,8 @@ def bench_adjoint_workload(H, torch, n=N_GRID, nsteps=100, reps=2):
     f = statistics.median(x[0] for x in res)
     a = statistics.median(x[1] for x in res)
     out = {"workload": f"{n}x{n} Bernoulli rain + talus slippage, per-cell Ks, {nsteps} steps",
-           "ckpt_every": tape.ckpt_every, "ms_forward": f, "ms_fwd_adjoint": a, "fwd_adjoint_over_forward_time": a / f,
+           "ckpt_every": tape.ckpt_every, "recomputed_steps": nsteps - tape.ckpt_every, "ms_forward": f,
+           "ms_fwd_adjoint": a, "fwd_adjoint_over_forward_time": a / f,
            "fwd_adjoint_cell_steps_per_s": n * n * nsteps / (a / 1e3),
            "gradient_finite": bool(torch.isfinite(dks).all() and torch.isfinite(db0).all())}
     tape.close()
@@ -398,7 +422,8 @@ def bench_large(H, torch, n=8192, fwd_steps=2000, adj_steps=512, nbatch=16, bn=1
     e2.record(st)
     e2.synchronize()
     f, a = e0.elapsed_time(e1), e0.elapsed_time(e2)
-    out["fwd_adjoint"] = {"steps": adj_steps, "ckpt_every": tape.ckpt_every, "ms_forward": f, "ms_fwd_adjoint": a,
+    out["fwd_adjoint"] = {"steps": adj_steps, "ckpt_every": tape.ckpt_every,
+                          "recomputed_steps": adj_steps - tape.ckpt_every, "ms_forward": f, "ms_fwd_adjoint": a,
                           "fwd_adjoint_over_forward_time": a / f,
                           "fwd_adjoint_cell_steps_per_s": n * n * adj_steps / (a / 1e3),
                           "gradient_finite": bool(torch.isfinite(dks).all() and torch.isfinite(db0).all())}
@@ -864,6 +889,11 @@ def main():
                 out = bench_terrain(H, torch, reps=args.steps, cpu_budget_s=budget)
             elif args.extra == "config1":
                 out = bench_config1(H, torch, cpu=budget > 0)
+            elif args.extra == "fd_check":  # the default line's check plus the FP64 reference adjoint
+                out = bench_adjoint(H, torch, reps=1, fit_kw=dict(iters=1, chunk=1),
+                                    reference_adjoint=True)["fd_check"]
+            elif args.extra == "large":
+                out = bench_large(H, torch)
             elif args.extra == "fp64_error":
                 out = bench_fp64_error(H, torch)
             elif args.extra == "fit_study":  # fit schedules on the inverse workload

@@ -1739,14 +1739,19 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
     DeviceGuard g(w->device);
     const size_t c = cells(w);
     // Checkpoints (nsteps/K states) plus segment buffers (K states and
-    // slots each), within half the free memory.  The backward recomputes
-    // every segment but the last once, nsteps - K steps in all, so HG_AUTO
-    // takes the longest interval that fits (K = nsteps: nothing is
-    // recomputed); tape memory is smallest near K = sqrt(7 nsteps / 11),
+    // slots each), within the free memory less a reserve (a tenth of it, at
+    // least 4 GiB, for the caller's later allocations).  The backward
+    // recomputes every segment but the last once, nsteps - K steps in all,
+    // so HG_AUTO takes the longest interval that fits (K = nsteps: nothing
+    // is recomputed); tape memory is smallest near K = sqrt(7 nsteps / 11),
     // the fallback when nothing fits.  A second segment buffer, when it
     // fits too, lets the recompute overlap the reverse sweep.
     size_t free_b = 0, total_b = 0;
-    const size_t budget = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess ? free_b / 2 : (size_t)-1;
+    size_t budget = (size_t)-1;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+        const size_t reserve = std::max<size_t>(free_b / 10, (size_t)4 << 30);
+        budget = free_b > reserve ? free_b - reserve : 0;
+    }
     int K = ckpt_every, nbuf = 1;
     if (K == HG_AUTO || K <= 0) {
         K = 0;
