@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <array>
 #include <memory>
 #include <mutex>
@@ -118,6 +119,7 @@ struct hg_world {
     hg::Tuning tuning;                     // autotuned fused-step variant
     float* red_f = nullptr;   // min/max partials + result
     double* red_d = nullptr;  // FP64 partials + result
+    std::vector<hg_tape*> tapes;     // live tapes of this world (freed with it)
     hg::Particles* parts = nullptr;  // particle mode: droplets and momentum map
     float4* r_hm = nullptr;          // ray-marcher: packed heightmap texels
     float2* r_sed = nullptr;         // ray-marcher: packed sediment texels
@@ -125,6 +127,10 @@ struct hg_world {
     float* r_rgb = nullptr;
     size_t r_pixels = 0;             // capacity of r_rgba / r_rgb
 };
+
+namespace hg {
+void release_tapes(hg_world* w);
+}  // namespace hg
 
 struct hg_batch {
     std::vector<hg_world*> worlds;
@@ -821,6 +827,7 @@ int hg_world_destroy(hg_world* w) {
     if (!w) return HG_OK;
     DeviceGuard g(w->device);
     cudaStreamSynchronize(w->stream);
+    release_tapes(w);
     free_world(w);
     delete w;
     return HG_OK;
@@ -1713,6 +1720,21 @@ void free_tape(hg_tape* t) {
     if (t->rstream) cudaStreamDestroy(t->rstream);
 }
 
+}  // namespace
+
+// A world that is destroyed before its tapes frees their device memory and
+// leaves each tape a husk: hg_tape_destroy then only deletes the handle, and
+// the tape's other entry points report HG_ERR_STATE.
+extern "C++" void hg::release_tapes(hg_world* w) {
+    for (hg_tape* t : w->tapes) {
+        free_tape(t);
+        t->w = nullptr;
+    }
+    w->tapes.clear();
+}
+
+namespace {
+
 // state fields of a world (current buffers) -> contiguous state at dst
 int copy_state_out(hg_world* w, float* dst, cudaStream_t st) {
     size_t c = cells(w);
@@ -1794,21 +1816,27 @@ int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out) {
         cudaGetLastError();
         return fail(code, std::string("tape allocation: ") + cudaGetErrorString(e));
     }
+    w->tapes.push_back(t);
     *out = t;
     return HG_OK;
 }
 
 int hg_tape_destroy(hg_tape* t) {
     if (!t) return HG_OK;
-    DeviceGuard g(t->w->device);
-    cudaStreamSynchronize(t->w->stream);
-    free_tape(t);
+    if (t->w) {  // else its world's destruction released the buffers already
+        DeviceGuard g(t->w->device);
+        cudaStreamSynchronize(t->w->stream);
+        auto& v = t->w->tapes;
+        v.erase(std::remove(v.begin(), v.end(), t), v.end());
+        free_tape(t);
+    }
     delete t;
     return HG_OK;
 }
 
 int hg_tape_info(const hg_tape* t, int* nsteps, int* ckpt_every) {
     if (!t) return fail(HG_ERR_INVALID, "null tape");
+    if (!t->w) return fail(HG_ERR_STATE, "the tape's world was destroyed");
     if (nsteps) *nsteps = t->nsteps;
     if (ckpt_every) *ckpt_every = t->K;
     return HG_OK;
@@ -1858,6 +1886,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
 int hg_forward(hg_tape* t) {
     Range nv_range("hg_forward");
     if (!t) return fail(HG_ERR_INVALID, "null tape");
+    if (!t->w) return fail(HG_ERR_STATE, "the tape's world was destroyed");
     hg_world* w = t->w;
     HG_CHECK_VALID(w);
     if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0) or the reference rain");
@@ -1893,6 +1922,7 @@ int hg_forward(hg_tape* t) {
 int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* dL_drock0) {
     Range nv_range("hg_backward");
     if (!t) return fail(HG_ERR_INVALID, "null tape");
+    if (!t->w) return fail(HG_ERR_STATE, "the tape's world was destroyed");
     if (!t->recorded) return fail(HG_ERR_STATE, "hg_forward has not recorded this tape");
     if (!dL_drock_final) return fail(HG_ERR_INVALID, "null final-rock adjoint");
     hg_world* w = t->w;

@@ -11,7 +11,9 @@ Errors raise HydrogenError carrying the library's status code and message.
 The library must be built (build.build()); importing this module without it
 raises ImportError: there is no CPU fallback.
 """
+import atexit
 import ctypes
+import weakref
 import math
 import os
 
@@ -291,6 +293,23 @@ def bernoulli_threshold(p):
     return int(min(max(t, 0), 4294967295))
 
 
+# Live handles, closed at interpreter exit dependents first (tapes and
+# batches before the worlds they use) while the CUDA runtime is still up;
+# garbage collection of reference cycles would otherwise finalise them in
+# any order.
+_live = {"tapes": weakref.WeakSet(), "batches": weakref.WeakSet(), "worlds": weakref.WeakSet()}
+
+
+@atexit.register
+def _close_all():
+    for kind in ("tapes", "batches", "worlds"):
+        for obj in list(_live[kind]):
+            try:
+                obj.close()
+            except Exception:
+                pass
+
+
 class World:
     """An n x n erosion world on the current CUDA device."""
 
@@ -299,9 +318,13 @@ class World:
         check(lib.hg_world_create(n, layers, ctypes.byref(h)))
         self.h = h
         self.n = n
+        self._tapes = weakref.WeakSet()
+        _live["worlds"].add(self)
 
     def close(self):
         if self.h:
+            for t in list(self._tapes):  # a tape's handle before its world's
+                t.close()
             lib.hg_world_destroy(self.h)
             self.h = None
 
@@ -440,6 +463,8 @@ class Tape:
         check(lib.hg_tape_create(world.h, nsteps, ckpt_every, ctypes.byref(h)))
         self.h = h
         self.world = world
+        world._tapes.add(self)
+        _live["tapes"].add(self)
 
     def close(self):
         if self.h:
@@ -516,6 +541,7 @@ class Batch:
         h = ctypes.c_void_p()
         check(lib.hg_batch_create(arr, len(self.worlds), ctypes.byref(h)))
         self.h = h
+        _live["batches"].add(self)
 
     def close(self):
         if self.h:

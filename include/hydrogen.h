@@ -385,12 +385,15 @@ int hg_world_totals(hg_world* w, double out[3]);
  * passes; not smoothing), for fitting the per-cell rock solubility and the
  * initial rock heights.  A tape records nsteps steps of w with a checkpoint
  * of the carried fields every ckpt_every steps (HG_AUTO: the longest
- * interval whose tape fits in half the free device memory, up to nsteps,
- * when nothing is recomputed); hg_backward recomputes each segment but the
- * last from its checkpoint and runs the reverse kernels.  Subgradients at max/min/clamp
- * and at the dissolve/deposit branches: the taken branch's derivative.
- * The world's settings and per-cell Ks must not change between hg_forward
- * and hg_backward. */
+ * interval whose tape fits in the free device memory less a reserve of a
+ * tenth of it, at least 4 GiB; up to nsteps, when nothing is recomputed);
+ * hg_backward recomputes each segment but the last from its checkpoint and
+ * runs the reverse kernels.  Subgradients at max/min/clamp and at the
+ * dissolve/deposit branches: the taken branch's derivative.  The world's
+ * settings and per-cell Ks must not change between hg_forward and
+ * hg_backward.  Destroying a world frees the device memory of its live
+ * tapes; such a tape then answers HG_ERR_STATE, and hg_tape_destroy only
+ * releases its handle. */
 typedef struct hg_tape hg_tape;
 int hg_tape_create(hg_world* w, int nsteps, int ckpt_every, hg_tape** out);
 int hg_tape_destroy(hg_tape* t);
