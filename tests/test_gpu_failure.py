@@ -65,6 +65,24 @@ def test_timeout_leaves_the_world_undefined_until_reinitialised():
     assert np.array_equal(w.download("rock"), ref.download("rock"))
 
 
+def test_tape_outliving_its_world():
+    """A world destroyed before its tape frees the tape's device memory; the
+    tape then reports HG_ERR_STATE and its own destruction only drops the
+    handle (through the C ABI directly, past the wrapper's ordering)."""
+    import ctypes
+    w = H.World(64)
+    w.init_heightmap(H.noise(seed=1))
+    H.configure(w, "config1")
+    t = ctypes.c_void_p()
+    H.check(H.lib.hg_tape_create(w.h, 4, 2, ctypes.byref(t)))
+    H.check(H.lib.hg_world_destroy(w.h))
+    w.h = None
+    assert H.lib.hg_forward(t) == -7
+    a, b = ctypes.c_int(), ctypes.c_int()
+    assert H.lib.hg_tape_info(t, ctypes.byref(a), ctypes.byref(b)) == -7
+    H.check(H.lib.hg_tape_destroy(t))
+
+
 def two_layer_world(n):
     s = H.ErosionSettings()
     H.check(H.lib.hg_default_erosion_settings(ctypes.byref(s)))
