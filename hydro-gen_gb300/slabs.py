@@ -1,0 +1,142 @@
+"""Row-slab decomposition of one world over ranks: the schedule of one step.
+
+The reference dispatches every pass over the whole grid at once
+(src/erosion.cpp:92-101, 158-200).  Split over R ranks, rank r owns rows
+[lo_r, hi_r) of an n x n world and computes only those; before each pass it
+needs its neighbours' rows of the fields that pass reads around a cell:
+
+  pass                     reads outside the cell            halo rows
+  rain                     nothing                           0
+  hydro_flux               total height, flux (4-nbhd)       1 of height and flux
+  hydro_erosion            total height (4-nbhd, normal)     1 of height
+  sediment_transport       eroded sediment at the back-trace the back-trace's reach
+  thermal_erosion (layer)  total height (8-nbhd)             1 of height
+  thermal_transport        outflows (8-nbhd)                 1 of both outflow maps
+  smoothing                total height (4-nbhd)             1 of height
+
+The sediment back-trace reach |v| dt is unbounded (velocity divides by the
+water depth), so after the flux pass every rank takes the largest reach over
+its rows, the ranks agree on the maximum (an all-reduce), and the eroded
+sediment's halo is exchanged that deep when it fits inside the neighbours'
+slabs and `halo_max`, else every rank gathers the whole field (all-gather):
+the fallback the unbounded reach needs.  Halos come from the two neighbours
+only; no other data moves.
+
+This module is the host-side schedule only.  It drives any `stepper` that
+runs one pass over the owned rows and reads and writes rows of a field
+(`run_pass`, `get_rows`, `set_rows`, `max_reach_rows`), through
+torch.distributed collectives on CPU tensors (gloo; a GPU stepper would pass
+device tensors to NCCL).  The tests drive it with the float oracle's passes
+restricted to a slab, bit for bit against one process stepping the whole
+world (tests/test_slabs_gloo.py).
+"""
+import numpy as np
+
+# (pass, layer, [(field, halo rows or "reach"), ...]) in the step's order
+STEP_PLAN = [
+    ("rain", 0, []),
+    ("flux", 0, [("height", 1), ("flux", 1)]),
+    ("erosion", 0, [("height", 1)]),
+    ("sediment", 0, [("sed", "reach")]),
+    ("thermal_flux", 0, [("height", 1)]),
+    ("thermal_transport", 0, [("thc", 1), ("thd", 1)]),
+    ("thermal_flux", 1, [("height", 1)]),
+    ("thermal_transport", 1, [("thc", 1), ("thd", 1)]),
+    ("smoothing", 0, [("height", 1)]),
+]
+
+
+def slab_rows(n, nranks):
+    """Row ranges [lo, hi) of an even split of n rows over nranks ranks."""
+    if nranks < 1 or nranks > n:
+        raise ValueError("need 1 <= ranks <= rows")
+    base, extra = divmod(n, nranks)
+    out, lo = [], 0
+    for r in range(nranks):
+        hi = lo + base + (1 if r < extra else 0)
+        out.append((lo, hi))
+        lo = hi
+    return out
+
+
+def passes_of_step(step1, settings, rain_period, rain_on=True):
+    """The passes one step runs (the reference's cadence and the identity
+    passes it skips: a talus layer with no slippage, smoothing with
+    Kspeed[1] == 0): the plan's entries for step number step1 (1-based)."""
+    out = []
+    for name, layer, halos in STEP_PLAN:
+        if name == "rain" and not (rain_on and rain_period > 0 and step1 % rain_period == 0):
+            continue
+        if name.startswith("thermal") and settings.Kspeed[layer] == 0.0:
+            continue
+        if name == "smoothing" and settings.Kspeed[1] == 0.0:
+            continue
+        out.append((name, layer, halos))
+    return out
+
+
+class SlabComm:
+    """Halo exchange and gather of row blocks between the ranks of a slab
+    decomposition (torch.distributed, any backend)."""
+
+    def __init__(self, dist, rank, nranks, rows, n, channels=4):
+        import torch
+        self.torch = torch
+        self.dist = dist
+        self.rank, self.nranks, self.rows, self.n, self.ch = rank, nranks, rows, n, channels
+        self.min_rows = min(hi - lo for lo, hi in rows)
+        self.gathers = 0
+        self.exchanges = 0
+
+    def agree_max(self, value):
+        t = self.torch.tensor([float(value)], dtype=self.torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def exchange(self, stepper, field, depth):
+        """Refresh `depth` rows on each side of the own slab from the
+        neighbours (depth <= the smallest slab)."""
+        torch = self.torch
+        lo, hi = self.rows[self.rank]
+        blk = np.zeros((2, depth, self.n, self.ch))
+        blk[0] = stepper.get_rows(field, lo, lo + depth)  # to the rank below
+        blk[1] = stepper.get_rows(field, hi - depth, hi)  # to the rank above
+        mine = torch.from_numpy(blk)
+        allb = [torch.empty_like(mine) for _ in range(self.nranks)]
+        self.dist.all_gather(allb, mine)
+        if self.rank > 0:  # rows [lo - depth, lo): the top rows of rank - 1
+            stepper.set_rows(field, lo - depth, allb[self.rank - 1][1].numpy())
+        if self.rank < self.nranks - 1:  # rows [hi, hi + depth): the bottom rows of rank + 1
+            stepper.set_rows(field, hi, allb[self.rank + 1][0].numpy())
+        self.exchanges += 1
+
+    def gather(self, stepper, field):
+        """Every rank receives every row of the field."""
+        torch = self.torch
+        lo, hi = self.rows[self.rank]
+        h = max(b - a for a, b in self.rows)
+        blk = np.zeros((h, self.n, self.ch))
+        blk[: hi - lo] = stepper.get_rows(field, lo, hi)
+        mine = torch.from_numpy(blk)
+        allb = [torch.empty_like(mine) for _ in range(self.nranks)]
+        self.dist.all_gather(allb, mine)
+        for r, (a, b) in enumerate(self.rows):
+            if r != self.rank:
+                stepper.set_rows(field, a, allb[r][: b - a].numpy())
+        self.gathers += 1
+
+
+def slab_step(stepper, comm, step1, settings, rain_period, halo_max=8, rain_on=True):
+    """One step of the owned rows: each pass after the halos it reads."""
+    for name, layer, halos in passes_of_step(step1, settings, rain_period, rain_on):
+        for field, depth in halos:
+            if depth == "reach":
+                reach = int(comm.agree_max(stepper.max_reach_rows()))
+                if reach <= min(halo_max, comm.min_rows):
+                    if reach > 0:
+                        comm.exchange(stepper, field, reach)
+                else:
+                    comm.gather(stepper, field)
+            else:
+                comm.exchange(stepper, field, depth)
+        stepper.run_pass(name, layer)

@@ -48,6 +48,7 @@
 #include <cstring>
 #include <cstddef>
 #include <vector>
+#include <type_traits>
 #include <algorithm>
 #ifdef _OPENMP
 #include <omp.h>
@@ -219,6 +220,11 @@ template <typename T> struct World {
     }
     size_t id(int x, int y) const { return (size_t)y * n + x; }
     bool inb(int x, int y) const { return x >= 0 && x < n && y >= 0 && y < n; }
+    // rows the grid passes compute ([row_lo, row_end()); all by default): a
+    // slab of a row decomposition computes only its own rows, its halo rows
+    // are copied in between passes
+    int row_lo = 0, row_hi = -1;
+    int row_end() const { return row_hi < 0 ? n : row_hi; }
 };
 
 #define OMP_ROWS _Pragma("omp parallel for schedule(static)")
@@ -235,7 +241,7 @@ template <typename T> void rain_pass(World<T>& w, const OracleOptions& o, uint64
     auto& dst = w.height.wr();
     const T amount = T(o.rain_amount);
     OMP_ROWS
-    for (int y = 0; y < w.n; ++y)
+    for (int y = w.row_lo; y < w.row_end(); ++y)
         for (int x = 0; x < w.n; ++x) {
             V4<T> terr = src[w.id(x, y)];
             T incr = T(0);
@@ -263,7 +269,7 @@ template <typename T> void flux_pass(World<T>& w, const OracleErosion& s) {
     const T FAR = T(999999999999.0);
     const int n = w.n;
     OMP_ROWS
-    for (int y = 0; y < n; ++y)
+    for (int y = w.row_lo; y < w.row_end(); ++y)
         for (int x = 0; x < n; ++x) {
             auto wh = [&](int xx, int yy) -> T { return w.inb(xx, yy) ? H[w.id(xx, yy)].w : FAR; };
             auto gf = [&](int xx, int yy) -> V4<T> { return w.inb(xx, yy) ? F[w.id(xx, yy)] : V4<T>{}; };
@@ -323,7 +329,7 @@ template <typename T> void erosion_pass(World<T>& w, const OracleErosion& s) {
     const bool cell_ks = !w.ks.empty();
     const int n = w.n;
     OMP_ROWS
-    for (int y = 0; y < n; ++y)
+    for (int y = w.row_lo; y < w.row_end(); ++y)
         for (int x = 0; x < n; ++x) {
             auto ld = [&](int xx, int yy) -> V4<T> { return w.inb(xx, yy) ? H[w.id(xx, yy)] : V4<T>{}; };
             V4<T> vel = VL[w.id(x, y)];
@@ -410,7 +416,7 @@ template <typename T> void sediment_pass(World<T>& w, const OracleErosion& s) {
     const int n = w.n;
     const T maxc = T(n - 1);
     OMP_ROWS
-    for (int y = 0; y < n; ++y)
+    for (int y = w.row_lo; y < w.row_end(); ++y)
         for (int x = 0; x < n; ++x) {
             V4<T> vel = VL[w.id(x, y)];
             T bx = T(x) - vel.x * dt;
@@ -440,7 +446,7 @@ template <typename T> void thermal_flux_pass(World<T>& w, const OracleErosion& s
     const int ox[2][4] = {{-1, 1, 0, 0}, {-1, 1, -1, 1}};
     const int oy[2][4] = {{0, 0, 1, -1}, {1, 1, -1, -1}};
     OMP_ROWS
-    for (int y = 0; y < n; ++y)
+    for (int y = w.row_lo; y < w.row_end(); ++y)
         for (int x = 0; x < n; ++x) {
             auto gh = [&](int xx, int yy) -> V4<T> {
                 if (!w.inb(xx, yy)) return V4<T>{FAR, FAR, FAR, FAR};
@@ -495,7 +501,7 @@ template <typename T> void thermal_transport_pass(World<T>& w, int layer) {
     auto& Ho = w.height.wr();
     const int n = w.n;
     OMP_ROWS
-    for (int y = 0; y < n; ++y)
+    for (int y = w.row_lo; y < w.row_end(); ++y)
         for (int x = 0; x < n; ++x) {
             auto g = [&](const std::vector<V4<T>>& img, int xx, int yy) -> V4<T> {
                 return w.inb(xx, yy) ? img[w.id(xx, yy)] : V4<T>{};
@@ -529,7 +535,7 @@ template <typename T> void smoothing_pass(World<T>& w, const OracleErosion& s) {
     const T d_time = T(s.d_t);
     const int n = w.n;
     OMP_ROWS
-    for (int y = 0; y < n; ++y)
+    for (int y = w.row_lo; y < w.row_end(); ++y)
         for (int x = 0; x < n; ++x) {
             V4<T> terrain = H[w.id(x, y)];
             T tr = terrain.x, tg = terrain.y;
@@ -984,6 +990,48 @@ int hgo_particles_get(void* p, float* state8, uint32_t* iters, int32_t* kill) {
 }
 
 // Single passes, for the per-pass unit tests.
+// Restricts the grid passes to rows [lo, hi) (hi < 0: every row).
+int hgo_set_rows(void* p, int lo, int hi) {
+    auto* h = (OracleHandle*)p;
+    const int n = h->wd ? h->wd->n : h->wf->n;
+    if (lo < 0 || lo > n || (hi >= 0 && (hi < lo || hi > n))) return -1;
+    if (h->wd) { h->wd->row_lo = lo; h->wd->row_hi = hi; }
+    else { h->wf->row_lo = lo; h->wf->row_hi = hi; }
+    return 0;
+}
+
+// Rows [y0, y1) of the current (read) texture `tex` (0 height, 1 flux,
+// 2 velocity, 3 sediment, 4 thermal cross, 5 thermal diagonal), four
+// channels per cell, to (write == 0) or from (write != 0) buf as doubles
+// (float worlds convert exactly).  A slab decomposition's halo exchange.
+int hgo_tex_rows(void* p, int tex, int y0, int y1, double* buf, int write) {
+    auto* h = (OracleHandle*)p;
+    auto run = [&](auto& w) -> int {
+        using T = typename std::remove_reference<decltype(w.height.tex[0][0].x)>::type;
+        if (y0 < 0 || y1 > w.n || y0 > y1) return -1;
+        decltype(&w.height) pr = nullptr;
+        switch (tex) {
+            case 0: pr = &w.height; break;
+            case 1: pr = &w.flux; break;
+            case 2: pr = &w.vel; break;
+            case 3: pr = &w.sed; break;
+            case 4: pr = &w.thc; break;
+            case 5: pr = &w.thd; break;
+            default: return -1;
+        }
+        auto& t = pr->tex[pr->r];
+        for (int y = y0; y < y1; ++y)
+            for (int x = 0; x < w.n; ++x) {
+                auto& v = t[w.id(x, y)];
+                double* q = buf + 4 * ((size_t)(y - y0) * w.n + x);
+                if (write) { v.x = (T)q[0]; v.y = (T)q[1]; v.z = (T)q[2]; v.w = (T)q[3]; }
+                else { q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w; }
+            }
+        return 0;
+    };
+    return h->wd ? run(*h->wd) : run(*h->wf);
+}
+
 int hgo_pass(void* p, const OracleErosion* s, const OracleOptions* o, int which, int layer) {
     auto* h = (OracleHandle*)p;
     auto run = [&](auto& w) {

@@ -68,6 +68,8 @@ def _load():
         "hgo_step": (ctypes.c_int, [P, ctypes.POINTER(OracleErosion), ctypes.POINTER(OracleOptions), ctypes.c_int]),
         "hgo_pass": (ctypes.c_int, [P, ctypes.POINTER(OracleErosion), ctypes.POINTER(OracleOptions), ctypes.c_int,
                                     ctypes.c_int]),
+        "hgo_set_rows": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "hgo_tex_rows": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]),
         "hgo_get_thermal": (ctypes.c_int, [P, P, P]),
         "hgo_totals": (None, [P, ctypes.POINTER(ctypes.c_double)]),
         "hgo_atanf": (ctypes.c_float, [ctypes.c_float]),
@@ -206,6 +208,22 @@ class OracleWorld:
     def run_pass(self, name, settings, opts=None, layer=0):
         opts = opts or options()
         assert lib.hgo_pass(self.h, ctypes.byref(settings), ctypes.byref(opts), PASSES[name], layer) == 0
+
+    def set_rows(self, lo=0, hi=-1):
+        """Restrict the grid passes to rows [lo, hi) (hi = -1: all rows)."""
+        assert lib.hgo_set_rows(self.h, lo, hi) == 0
+
+    TEXTURES = {"height": 0, "flux": 1, "vel": 2, "sed": 3, "thc": 4, "thd": 5}
+
+    def tex_rows(self, tex, y0, y1):
+        """Rows [y0, y1) of a current texture as (rows, n, 4) doubles."""
+        a = np.empty((y1 - y0, self.n, 4), dtype=np.float64)
+        assert lib.hgo_tex_rows(self.h, self.TEXTURES[tex], y0, y1, a.ctypes.data, 0) == 0
+        return a
+
+    def set_tex_rows(self, tex, y0, rows):
+        a = np.ascontiguousarray(rows, dtype=np.float64)
+        assert lib.hgo_tex_rows(self.h, self.TEXTURES[tex], y0, y0 + a.shape[0], a.ctypes.data, 1) == 0
 
     def particles_init(self, count):
         assert lib.hgo_particles_init(self.h, count) == 0
