@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and batch measurements")
     ap.add_argument("--extra", choices=["particles", "render", "two_layer", "terrain", "adjoint", "adjoint_thermal",
-                                        "batch", "config1", "fp64_error", "fit_study", "large", "fd_check"],
+                                        "batch", "batch_class", "config1", "fp64_error", "fit_study", "large",
+                                        "fd_check"],
                     default=None,
                     help="run only this extra measurement (--steps timed steps or frames, --warmup warm-up) "
                          "and print its JSON; for profiling captures")
@@ -597,6 +598,47 @@ def bench_batch(H, torch, count=64, nsteps=200, warmup=16):
     out["one_launch_over_per_terrain"] = out["one_launch_cell_steps_per_s"] / out["per_terrain_cell_steps_per_s"]
     for w in ws:
         w.close()
+    out["size_classes"] = batch_size_classes(H, torch)
+    single = out["size_classes"]["4096"]["per_terrain_ps_per_cell_step"]  # the single-world kernels
+    out["one_launch_over_single_world_rate"] = out["one_launch_cell_steps_per_s"] * single * 1e-12
+    return out
+
+
+CLASS_TERRAINS = {256: 128, 512: 64, 1024: 16, 2048: 4, 4096: 1}
+
+
+def batch_size_classes(H, torch, nsteps=100, warmup=16, sides=(256, 512, 1024, 2048, 4096)):
+    """The per-cell cost of each terrain size of the ragged batch on its own:
+    a batch of equal terrains per side (config-2 physics, Bernoulli rain,
+    64 x 16 tiles, graph replay) as one table launch and as each terrain's own
+    launches; at 4096² one world, whose own launches are the single-world
+    kernels.  ps per cell-step."""
+    out = {}
+    for side in sides:
+        count = CLASS_TERRAINS.get(side, 1)
+        ws = []
+        for i in range(count):
+            w = H.World(side)
+            w.init_heightmap(H.noise(seed=i))
+            H.configure(w, "config2")
+            w.set_options(H.options(H.RAIN_BERNOULLI, p=0.001, seed=i, terrain_id=i, tile=(64, 16), graph=1))
+            ws.append(w)
+        cells = count * side * side
+        b = H.Batch(ws)
+        row = {"terrains": count}
+        for key, mode in (("one_launch", H.MODE_FUSED), ("per_terrain", H.MODE_FUSED_PER_WORLD)):
+            b.step(warmup, mode)
+            b.sync()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.step(nsteps, mode)
+            b.sync()
+            torch.cuda.synchronize()
+            row[key + "_ps_per_cell_step"] = 1e12 * (time.perf_counter() - t0) / (nsteps * cells)
+        b.close()
+        for w in ws:
+            w.close()
+        out[str(side)] = row
     return out
 
 
@@ -910,6 +952,8 @@ def main():
                                     reps=max(1, args.warmup))
             elif args.extra == "batch":  # --steps timed steps, --warmup warm-up steps
                 out = bench_batch(H, torch, nsteps=args.steps, warmup=args.warmup)
+            elif args.extra == "batch_class":  # one size class of the batch: --n side
+                out = batch_size_classes(H, torch, nsteps=args.steps, warmup=args.warmup, sides=(args.n,))
             elif args.extra == "adjoint_thermal":  # --n grid, --steps taped steps, --warmup repetitions
                 out = bench_adjoint_workload(H, torch, n=args.n, nsteps=args.steps, reps=max(1, args.warmup))
             else:

@@ -14,6 +14,10 @@
 // intermediate traffic (eroded rock and sediment written and read once) and
 // saves recomputing flux and erosion on a halo ring.
 //
+// Edge tiles (whose box leaves the grid) run either their own copy of the
+// tile code or the inner tiles' code with block-uniform edge branches: the
+// latter for batches and worlds below 4096² (see hydro_block).
+//
 // Both kernels are table driven: one launch covers every tile of any number
 // of worlds ("terrains") of different sizes and settings.  A block finds its
 // terrain by binary search over the terrains' first tiles and reads the terrain's record (step constants, rain
@@ -104,9 +108,12 @@ __device__ __forceinline__ RainStep rain_for(const RainBase& rb, unsigned long l
 // ---------------------------------------------------------------------------
 // k_hydro
 // ---------------------------------------------------------------------------
-template <int TH, bool EDGE>
+// EM: 0 inner tile, 1 edge tile (each its own code), 2 either, told at run
+// time by edge_rt (one code path for both)
+template <int TH, int EM>
 __device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorMap* maps, float* sm, uint64_t* bar,
-                                           int tx0, int ty0, int* err) {
+                                           int tx0, int ty0, bool edge_rt, int* err) {
+    const bool EDGE = EM == 2 ? edge_rt : EM == 1;
     using G = Geo<TH>;
     constexpr int NTH = G::NTH, H_RC = G::H_RC, H_RH = G::H_RH;
     const StepConsts& c = td.c;
@@ -156,6 +163,16 @@ __device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorM
             st4(D + ry * RW + rx, d);
         }
     }
+    if (EDGE) {  // water outside the grid (zero-filled by the copy) becomes the shader's
+                 // out-of-range height: with rock 0 there, the neighbour's total height
+                 // rock + water is exactly FAR_HEIGHT; rock 0 and flux 0 outside are
+                 // what the shader reads there too, so neighbour reads need no test
+        float* Dw = sm + H_D * H_RC;
+        for (int i = tid; i < G::H_BOX; i += NTH) {
+            const int gx = gx0 + i % RW, gy = gy0 + i / RW;
+            if (gx < 0 || gx >= n || gy < 0 || gy >= n) Dw[i] = FAR_HEIGHT;
+        }
+    }
     __syncthreads();
 
     const float* B = sm + H_B * H_RC;
@@ -172,25 +189,21 @@ __device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorM
         const int x = tx0 + ix, y = ty0 + iy;
         const int si = (1 + iy) * RW + HX + ix;
         const size_t gi = (size_t)y * n + x;
-        const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
-        const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
+        // neighbours outside the grid read rock 0, flux 0 and total height
+        // FAR_HEIGHT from the tile (see the fill above); the closed-boundary
+        // outflow zeroing runs in edge tiles
         float b = B[si], d1 = D[si];
         float bl = B[si - 1], br = B[si + 1], bb = B[si - RW], bt = B[si + RW];
         float w_c = b + d1;
-        float wl = has_l ? bl + D[si - 1] : FAR_HEIGHT;
-        float wr = has_r ? br + D[si + 1] : FAR_HEIGHT;
-        float wt = has_t ? bt + D[si + RW] : FAR_HEIGHT;
-        float wb = has_b ? bb + D[si - RW] : FAR_HEIGHT;
-        float inl = has_l ? FR[si - 1] : 0.0f;
-        float inr = has_r ? FL[si + 1] : 0.0f;
-        float int_ = has_t ? FB[si + RW] : 0.0f;
-        float inb = has_b ? FT[si - RW] : 0.0f;
-        FluxOut o = cell_flux(c, x, y, w_c, d1, FL[si], FR[si], FT[si], FB[si], wl, wr, wt, wb, inl, inr, int_, inb,
-                              EDGE);
+        float wl = bl + D[si - 1];
+        float wr = br + D[si + 1];
+        float wt = bt + D[si + RW];
+        float wb = bb + D[si - RW];
+        FluxOut o = cell_flux(c, x, y, w_c, d1, FL[si], FR[si], FT[si], FB[si], wl, wr, wt, wb, FR[si - 1], FL[si + 1],
+                              FB[si + RW], FT[si - RW], EDGE);
         float s = S[si];
         float Kls0 = c.ks_field ? c.dt * __ldg(c.ks_field + gi) : c.Kls0;
-        cell_erosion(c, Kls0, o.u, o.v, o.vz, b, s, has_r ? br : 0.0f, has_l ? bl : 0.0f, has_b ? bb : 0.0f,
-                     has_t ? bt : 0.0f);
+        cell_erosion(c, Kls0, o.u, o.v, o.vz, b, s, br, bl, bb, bt);
         td.out[S_FL][gi] = o.fl;
         td.out[S_FR][gi] = o.fr;
         td.out[S_FT][gi] = o.ft;
@@ -203,7 +216,7 @@ __device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorM
     }
 }
 
-template <int TH>
+template <int TH, bool SPLIT>
 __device__ __forceinline__ void hydro_block(const TerrainHot& td, const CUtensorMap* maps, int tile, int* err) {
     using G = Geo<TH>;
     __shared__ __align__(128) float sm[H_N * G::H_RC];
@@ -213,8 +226,14 @@ __device__ __forceinline__ void hydro_block(const TerrainHot& td, const CUtensor
     const int n = td.c.n;
     const int tx0 = (tile % td.tiles_x) * TW, ty0 = (tile / td.tiles_x) * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 1 >= 0 && ty0 + TH + 1 <= n;
-    if (inner) hydro_tile<TH, false>(td, maps, sm, &bar, tx0, ty0, err);
-    else hydro_tile<TH, true>(td, maps, sm, &bar, tx0, ty0, err);
+    // Small terrains are mostly edge tiles, interleaved with inner ones on
+    // every SM: !SPLIT runs one code path for both (two unrolled copies
+    // missed in the instruction cache: 4.6 stalls per issue on an empty
+    // instruction buffer, 11 % more time at 256²).  A large world is almost
+    // all inner tiles and keeps a copy specialised for them (SPLIT).
+    if (!SPLIT) hydro_tile<TH, 2>(td, maps, sm, &bar, tx0, ty0, !inner, err);
+    else if (inner) hydro_tile<TH, 0>(td, maps, sm, &bar, tx0, ty0, false, err);
+    else hydro_tile<TH, 1>(td, maps, sm, &bar, tx0, ty0, true, err);
 }
 
 // Batch form: the terrain records are a kernel parameter (constant bank),
@@ -223,14 +242,14 @@ template <int TH>
 __global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro(const __grid_constant__ BatchParams bp,
                                                         const CUtensorMap* __restrict__ maps, int* err) {
     const int t = find_terrain(bp.tile0, bp.nterr, blockIdx.x);
-    hydro_block<TH>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
+    hydro_block<TH, false>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
 }
 
 // Single-world form: the whole descriptor, tensor maps included, is a kernel
-// parameter.
-template <int TH>
+// parameter.  SPLIT as for hydro_block: the host picks it by world size.
+template <int TH, bool SPLIT>
 __global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro1(const __grid_constant__ TerrainDesc td, int* err) {
-    hydro_block<TH>(td.h, td.maps, blockIdx.x, err);
+    hydro_block<TH, SPLIT>(td.h, td.maps, blockIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -261,18 +280,19 @@ __device__ __forceinline__ void talus_nb(const float* be, int rx, int ry, int gx
 }
 
 // Talus outflows of two ring cells at once (lanes .x, .y) from the staged
-// eroded rock (row 0 = global row gy0, column 0 = global column gx0); a
-// cell outside the grid has none.
-template <bool EDGE>
+// eroded rock (row 0 = global row gy0, column 0 = global column gx0; at the
+// grid's edge the box holds FAR_HEIGHT outside the grid, so a neighbour
+// outside reads the shader's out-of-range height); a cell outside the grid
+// has none.
 __device__ __forceinline__ void pair_outflows(const StepConsts& c, const float* be, int rxa, int rya, int rxb,
-                                              int ryb, int gx0, int gy0, float2 o[8]) {
+                                              int ryb, int gx0, int gy0, bool EDGE, float2 o[8]) {
     const int n = c.n;
     const int gxa = gx0 + rxa, gya = gy0 + rya, gxb = gx0 + rxb, gyb = gy0 + ryb;
     const bool ina = !EDGE || (gxa >= 0 && gxa < n && gya >= 0 && gya < n);
     const bool inb = !EDGE || (gxb >= 0 && gxb < n && gyb >= 0 && gyb < n);
-    float na[8], nbb[8];
-    talus_nb<EDGE>(be, rxa, rya, gxa, gya, n, na);
-    talus_nb<EDGE>(be, rxb, ryb, gxb, gyb, n, nbb);
+    float na[8], nbb[8];  // the staged box holds FAR_HEIGHT outside the grid
+    talus_nb<false>(be, rxa, rya, gxa, gya, n, na);
+    talus_nb<false>(be, rxb, ryb, gxb, gyb, n, nbb);
     float2 nb2[8];
 #pragma unroll
     for (int d = 0; d < 8; ++d) nb2[d] = make_float2(na[d], nbb[d]);
@@ -286,20 +306,15 @@ __device__ __forceinline__ void pair_outflows(const StepConsts& c, const float* 
     }
 }
 
-// Talus outflows of the row group of four cells at region (rx0, ry), global
-// (x0, y), as two pairs (cells 0, 1 and 2, 3), stored to outf (direction
-// stride o_c, the group's first cell at oi); osum[h] receives pair h's
-// 0 - own[0] - ... - own[7].  A row outside the grid has none.
-template <bool EDGE>
-__device__ __forceinline__ void group_outflows(const StepConsts& c, const float* be, int rx0, int ry, int x0, int y,
-                                               float* outf, int o_c, int oi, float2 osum[2]) {
-    const int n = c.n;
+// Talus outflows of the row group of four cells at region (rx0, ry) (a row
+// of the tile, so inside the grid), as two pairs (cells 0, 1 and 2, 3),
+// stored to outf (direction stride o_c, the group's first cell at oi);
+// osum[h] receives pair h's 0 - own[0] - ... - own[7].
+__device__ __forceinline__ void group_outflows(const StepConsts& c, const float* be, int rx0, int ry, float* outf,
+                                               int o_c, int oi, float2 osum[2]) {
+    // the group's row is in the grid; outside it the box holds FAR_HEIGHT,
+    // so every neighbour is read from the box
     osum[0] = osum[1] = pf(0.0f);
-    if (EDGE && (y < 0 || y >= n)) {
-#pragma unroll
-        for (int d = 0; d < 8; ++d) st4(outf + d * o_c + oi, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
-        return;
-    }
     const int si = ry * RW + rx0;
     const float4 m4 = ld4(be + si - RW), c4 = ld4(be + si), p4 = ld4(be + si + RW);
     const float ml = be[si - RW - 1], mr = be[si - RW + 4];
@@ -308,17 +323,14 @@ __device__ __forceinline__ void group_outflows(const StepConsts& c, const float*
     float nb[4][8];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const int x = x0 + j;
-        const bool has_l = !EDGE || x > 0, has_r = !EDGE || x < n - 1;
-        const bool has_b = !EDGE || y > 0, has_t = !EDGE || y < n - 1;
-        nb[j][0] = has_l ? (j == 0 ? cl : at4(c4, j - 1)) : FAR_HEIGHT;
-        nb[j][1] = has_r ? (j == 3 ? cr : at4(c4, j + 1)) : FAR_HEIGHT;
-        nb[j][2] = has_t ? at4(p4, j) : FAR_HEIGHT;
-        nb[j][3] = has_b ? at4(m4, j) : FAR_HEIGHT;
-        nb[j][4] = (has_l && has_t) ? (j == 0 ? pl : at4(p4, j - 1)) : FAR_HEIGHT;
-        nb[j][5] = (has_r && has_t) ? (j == 3 ? pr : at4(p4, j + 1)) : FAR_HEIGHT;
-        nb[j][6] = (has_l && has_b) ? (j == 0 ? ml : at4(m4, j - 1)) : FAR_HEIGHT;
-        nb[j][7] = (has_r && has_b) ? (j == 3 ? mr : at4(m4, j + 1)) : FAR_HEIGHT;
+        nb[j][0] = j == 0 ? cl : at4(c4, j - 1);
+        nb[j][1] = j == 3 ? cr : at4(c4, j + 1);
+        nb[j][2] = at4(p4, j);
+        nb[j][3] = at4(m4, j);
+        nb[j][4] = j == 0 ? pl : at4(p4, j - 1);
+        nb[j][5] = j == 3 ? pr : at4(p4, j + 1);
+        nb[j][6] = j == 0 ? ml : at4(m4, j - 1);
+        nb[j][7] = j == 3 ? mr : at4(m4, j + 1);
     }
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -334,9 +346,10 @@ __device__ __forceinline__ void group_outflows(const StepConsts& c, const float*
     }
 }
 
-template <int TH, bool EDGE>
+template <int TH, int EM>  // EM as for hydro_tile
 __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUtensorMap* maps, float* be, float* outf,
-                                               uint64_t* bar, int tx0, int ty0, int* err) {
+                                               uint64_t* bar, int tx0, int ty0, bool edge_rt, int* err) {
+    const bool EDGE = EM == 2 ? edge_rt : EM == 1;
     using G = Geo<TH>;
     constexpr int O_C = G::O_C;
     const StepConsts& c = td.c;
@@ -393,6 +406,14 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
         mbar_wait(bar, 0);
         return;
     }
+    if (EDGE) {  // the box's cells outside the grid (zero-filled by the copy) become the
+                 // shader's out-of-range height, so every neighbour read needs no test
+        for (int i = tid; i < G::T_BOX; i += G::NTH) {
+            const int gx = gx0 + i % RW, gy = gy0 + i / RW;
+            if (gx < 0 || gx >= n || gy < 0 || gy >= n) be[i] = FAR_HEIGHT;
+        }
+        __syncthreads();
+    }
     // the taps' loads were issued with the tile's copy: mix them now, before
     // the outflows need the registers
     finish_sed();
@@ -407,7 +428,7 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
             else if (q < TW) { rxa = HX + 2 * (q - TW / 2); rya = TH + 2; rxb = rxa + 1; ryb = TH + 2; }
             else { rxa = HX - 1; rya = 1 + q - TW; rxb = HX + TW; ryb = rya; }
             float2 o2[8];
-            pair_outflows<EDGE>(c, be, rxa, rya, rxb, ryb, gx0, gy0, o2);
+            pair_outflows(c, be, rxa, rya, rxb, ryb, gx0, gy0, EDGE, o2);
             const int roa = (rya - 1) * RW + rxa, rob = (ryb - 1) * RW + rxb;
             if (q < TW) {  // horizontally adjacent: one 8-byte store per direction
 #pragma unroll
@@ -427,7 +448,7 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
     const int rx0 = HX + 4 * g, ry = 2 + iy;  // region coords of the group's first cell
     const int oi = (ry - 1) * RW + rx0;
     float2 osum[2];
-    group_outflows<EDGE>(c, be, rx0, ry, x0, y, outf, O_C, oi, osum);
+    group_outflows(c, be, rx0, ry, outf, O_C, oi, osum);
     __syncthreads();
     // ---- thermal_transport: own outflows out, neighbours' outflows in -------
     // (cell_thermal_apply's operations: in_flux = in[0] + ... + in[7] from 0,
@@ -491,7 +512,7 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
     }
 }
 
-template <int TH>
+template <int TH, bool SPLIT>
 __device__ __forceinline__ void transport_block(const TerrainHot& td, const CUtensorMap* maps, int tile, int* err) {
     using G = Geo<TH>;
     __shared__ __align__(128) float be[G::T_BOX];
@@ -502,8 +523,10 @@ __device__ __forceinline__ void transport_block(const TerrainHot& td, const CUte
     const int n = td.c.n;
     const int tx0 = (tile % td.tiles_x) * TW, ty0 = (tile / td.tiles_x) * TH;
     bool inner = tx0 - HX >= 0 && tx0 + TW + HX <= n && ty0 - 2 >= 0 && ty0 + TH + 2 <= n;
-    if (inner) transport_tile<TH, false>(td, maps, be, outf, &bar, tx0, ty0, err);
-    else transport_tile<TH, true>(td, maps, be, outf, &bar, tx0, ty0, err);
+    // one code path for a batch, an inner copy for a single world (see hydro_block)
+    if (!SPLIT) transport_tile<TH, 2>(td, maps, be, outf, &bar, tx0, ty0, !inner, err);
+    else if (inner) transport_tile<TH, 0>(td, maps, be, outf, &bar, tx0, ty0, false, err);
+    else transport_tile<TH, 1>(td, maps, be, outf, &bar, tx0, ty0, true, err);
     // k_hydro of this step has finished (stream order) and the next step's
     // k_hydro starts after this launch: advance the terrain's step counter
     if (tile == 0 && threadIdx.x == 0) *td.step += 1ull;
@@ -513,12 +536,12 @@ template <int TH>
 __global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport(const __grid_constant__ BatchParams bp,
                                                             const CUtensorMap* __restrict__ maps, int* err) {
     const int t = find_terrain(bp.tile0, bp.nterr, blockIdx.x);
-    transport_block<TH>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
+    transport_block<TH, false>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
 }
 
-template <int TH>
+template <int TH, bool SPLIT>
 __global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport1(const __grid_constant__ TerrainDesc td, int* err) {
-    transport_block<TH>(td.h, td.maps, blockIdx.x, err);
+    transport_block<TH, SPLIT>(td.h, td.maps, blockIdx.x, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -596,14 +619,26 @@ void launch_fused_table(const BatchParams& bp, const CUtensorMap* maps, int tota
     count_launch(2);
 }
 
+// Worlds from this side up keep separate inner and edge code (edge tiles are
+// under 4 % of a 4096² launch at tile height 16); smaller ones, where edge
+// tiles are 8 % (2048²) to 56 % (256²) of the launch, run one code path.
+constexpr int SPLIT_MIN_N = 4096;
+
+template <int TH, bool SPLIT>
+void launch_one(const TerrainDesc& td, int tiles, int* err, cudaStream_t st) {
+    k_hydro1<TH, SPLIT><<<tiles, Geo<TH>::NTH, 0, st>>>(td, err);
+    k_transport1<TH, SPLIT><<<tiles, Geo<TH>::NTH, 0, st>>>(td, err);
+}
+
 void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st) {
     const int tiles = fused_tiles(td.h.c.n, th);
+    const bool split = td.h.c.n >= SPLIT_MIN_N;
     if (th == 16) {
-        k_hydro1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);
-        k_transport1<16><<<tiles, Geo<16>::NTH, 0, st>>>(td, err);
+        if (split) launch_one<16, true>(td, tiles, err, st);
+        else launch_one<16, false>(td, tiles, err, st);
     } else {
-        k_hydro1<8><<<tiles, Geo<8>::NTH, 0, st>>>(td, err);
-        k_transport1<8><<<tiles, Geo<8>::NTH, 0, st>>>(td, err);
+        if (split) launch_one<8, true>(td, tiles, err, st);
+        else launch_one<8, false>(td, tiles, err, st);
     }
     count_launch(2);
 }

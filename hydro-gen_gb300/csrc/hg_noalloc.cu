@@ -10,50 +10,33 @@
 // live in the file-scope array below, sized for HG_NOALLOC_MAX_FIELDS
 // fields, which every GPU that loads the library holds until the process
 // exits.
-#include <mutex>
-
 #include "hg_internal.h"
 
 namespace hg {
 
 namespace {
 
-constexpr int kMaxDevices = 64;
 constexpr int kParts = 304;  // blocks of the partial-sum kernel (2 per SM on 152 SMs)
 
 // Partial sums: field f, block b at [f * kParts + b].  Each call writes every
 // partial it later reads, so nothing here needs to start at zero.
 static __device__ __align__(256) double g_noalloc_partials[HG_NOALLOC_MAX_FIELDS * kParts];
 
-double* g_partials_addr[kMaxDevices] = {};
-std::mutex g_setup_mutex;
-
 // The host-side name g_noalloc_partials is only a stand-in for the device
-// array; kernels need its device address, looked up once per device with
-// that device current.
-int partials_for_current_device(double** out, std::string& err) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+// array; kernels need its device address in the current context.  It is
+// looked up on every call (a table lookup once the module is loaded, no
+// allocation): a cached address would go stale when the context is
+// destroyed and made again (cudaDeviceReset) and the module reloads
+// elsewhere.
+int partials_for_current_context(double** out, std::string& err) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        err = std::string("cudaGetSymbolAddress(g_noalloc_partials): ") + cudaGetErrorString(e);
         return HG_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        err = "device ordinal out of range for the static scratch table";
-        return HG_ERR_UNSUPPORTED;
-    }
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_partials_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            err = std::string("cudaGetSymbolAddress(g_noalloc_partials): ") + cudaGetErrorString(e);
-            return HG_ERR_CUDA;
-        }
-        g_partials_addr[dev] = static_cast<double*>(p);
-    }
-    *out = g_partials_addr[dev];
+    *out = static_cast<double*>(p);
     return HG_OK;
 }
 
@@ -76,7 +59,7 @@ extern "C" int hg_field_totals_noalloc(const float* const* fields, int nfields, 
     }
     double* partials = nullptr;
     std::string err;
-    int rc = partials_for_current_device(&partials, err);
+    int rc = partials_for_current_context(&partials, err);
     if (rc != HG_OK) return hg_report_error(rc, err.c_str());
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     launch_sum_f64(pl, nfields, count, partials, kParts, out, st);

@@ -1201,6 +1201,13 @@ int hg_world_count_nonfinite(hg_world* w, uint64_t* count) {
         launch_count_nonfinite(w->dirt[0], c, d, w->stream);
         launch_count_nonfinite(w->sdirt[0], c, d, w->stream);
     }
+    if (w->parts) {  // the momentum map and every droplet's float state
+        const Particles& P = *w->parts;
+        for (int ch = 0; ch < 4; ++ch) launch_count_nonfinite(P.mom[0][ch], c, d, w->stream);
+        const Drops& dr = P.b.d;
+        for (float* f : {dr.px, dr.py, dr.vx, dr.vy, dr.vol, dr.s0, dr.s1, dr.sc})
+            launch_count_nonfinite(f, (size_t)P.count, d, w->stream);
+    }
     HG_CUDA(cudaGetLastError());
     unsigned long long h = 0;
     HG_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, w->stream));
@@ -1214,10 +1221,23 @@ int hg_world_poison_scratch(hg_world* w) {
     DeviceGuard g(w->device);
     const size_t b = cells(w) * sizeof(float);
     for (int f = 0; f < S_COUNT; ++f) HG_CUDA(cudaMemsetAsync(w->alt[f], 0xFF, b, w->stream));
-    for (float* p : {w->u, w->v, w->vz, w->s_ero, w->b_ero, w->dirt[1], w->sdirt[1]})
+    // u and v are carried (and counted) but belong to the grid step: a world
+    // with droplets keeps them, since the particle step neither reads nor
+    // writes them
+    for (float* p : {w->parts ? nullptr : w->u, w->parts ? nullptr : w->v, w->vz, w->s_ero, w->b_ero, w->dirt[1],
+                     w->sdirt[1]})
         if (p) HG_CUDA(cudaMemsetAsync(p, 0xFF, b, w->stream));
     for (float4* p : {w->tc, w->td})
         if (p) HG_CUDA(cudaMemsetAsync(p, 0xFF, 4 * b, w->stream));
+    if (w->parts) {
+        // the droplet records' sediment and layer mask (every record of a
+        // moving droplet writes both before the replay reads them); the
+        // momentum map's alternate is not scratch: border texels keep it
+        // from two steps back, as the reference's ping-pong does
+        const Particles& P = *w->parts;
+        HG_CUDA(cudaMemsetAsync(P.b.rec, 0xFF, 8 * (size_t)P.count * sizeof(float), w->stream));
+        HG_CUDA(cudaMemsetAsync(P.b.rec_mask, 0xFF, 4 * (size_t)P.count, w->stream));
+    }
     return HG_OK;
 }
 

@@ -470,10 +470,11 @@ int hg_world_load(hg_world* w, const char* path);
  * (a cudaStream_t, NULL for the legacy default stream); asynchronous.
  * Allocates nothing: the partial sums live in a fixed library-global device
  * array of HG_NOALLOC_MAX_FIELDS * 304 doubles (19,456 bytes) that each GPU
- * loading the library holds until the process exits.  The first call on a
- * device looks up that array's device address (once per device, with the
- * device current), so make the first call on each device before any stream
- * capture.  All calls share the one array: calls whose work overlaps on the
+ * loading the library holds until the process exits.  Each call looks up
+ * that array's address in the current context (so a cudaDeviceReset between
+ * calls is harmless); the first call in a context loads the library's module
+ * there, so make it before any stream capture in that context.  All calls
+ * share the one array: calls whose work overlaps on the
  * GPU (different streams, no ordering between them) race and give wrong
  * sums; order them on one stream or with events.  Rejects nfields outside
  * [1, HG_NOALLOC_MAX_FIELDS] with HG_ERR_INVALID. */
@@ -508,9 +509,12 @@ int hg_selftest_paired(uint64_t seed, uint64_t count, uint64_t mismatches[6]);
 int hg_selftest_report_timeout(hg_world* w);
 /* Coverage checks.  hg_world_poison_scratch fills every buffer a step writes
  * before reading (the alternate state buffers, velocity, the fused step's
- * hand-off and the thermal scratch) with NaN; hg_world_count_nonfinite
- * counts NaN and infinite values over the carried fields (rock, water,
- * sediment, four fluxes, u, v; dirt and dirt sediment in two-layer worlds).
+ * hand-off and the thermal scratch; in a world with droplets the droplet
+ * records' sediment and layer masks, and not the grid step's velocity,
+ * which the particle step leaves alone) with NaN; hg_world_count_nonfinite counts NaN
+ * and infinite values over the carried fields (rock, water, sediment, four
+ * fluxes, u, v; dirt and dirt sediment in two-layer worlds; the momentum map
+ * and the droplets' float state in particle mode).
  * After a step on a poisoned world the count is 0 exactly when the step
  * wrote every cell it owns.  Both are ordered on the world's stream; the
  * count synchronises. */

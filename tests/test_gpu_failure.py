@@ -128,3 +128,73 @@ def test_every_output_cell_is_written(layers, smooth, mode):
         fields += ["dirt", "sediment_dirt"]
     for f in fields:
         assert np.array_equal(a.download(f), b.download(f)), f
+
+
+def particle_world(n, count):
+    w = H.World(n, layers=2)
+    w.init_heightmap(H.noise(seed=2))
+    w.upload("dirt", np.full((n, n), 0.5, np.float32))
+    w.particles_init(count)
+    w.set_erosion(H.settings_particles())
+    w.set_options(H.options(H.RAIN_UNIFORM, seed=7))
+    return w
+
+
+def same_bits(x, y):
+    return np.array_equal(np.ascontiguousarray(x).view(np.uint32), np.ascontiguousarray(y).view(np.uint32))
+
+
+def test_every_output_cell_is_written_particles():
+    """Particle mode: the droplet records' sediment and layer masks and the
+    step's alternate buffers start each step as NaN; afterwards the fields,
+    the momentum map and every droplet equal an unpoisoned world's, bit for
+    bit, and hold no NaN (4096 droplets on 128² so texels share records)."""
+    n, count = 128, 4096
+    a, b = particle_world(n, count), particle_world(n, count)
+    bad = ctypes.c_uint64()
+    for _ in range(4):
+        H.check(H.lib.hg_world_poison_scratch(b.h))
+        b.step(1, H.MODE_PARTICLES)
+        H.check(H.lib.hg_world_count_nonfinite(b.h, ctypes.byref(bad)))
+        assert bad.value == 0
+    a.step(4, H.MODE_PARTICLES)
+    for f in ("rock", "dirt", "water", "momentum_x", "momentum_y"):
+        assert same_bits(a.download(f), b.download(f)), f
+    for x, y, name in zip(a.particles(), b.particles(), ("state", "iters", "kill")):
+        assert same_bits(x, y), name
+
+
+def test_every_output_cell_is_written_batch_table_launch():
+    """One table launch per fused kernel for two worlds of different sizes
+    (128² and 192², tile height 16, no graph: no autotuning, so every step is
+    the table form): each world's scratch is NaN before each batch step,
+    afterwards no carried field holds a NaN and both worlds equal an
+    unpoisoned batch's, bit for bit."""
+    def worlds():
+        out = []
+        for i, n in enumerate((128, 192)):
+            w = H.World(n)
+            w.init_heightmap(H.noise(seed=10 + i))
+            H.configure(w, "config2")
+            w.set_options(H.options(H.RAIN_BERNOULLI, p=0.02, seed=i, terrain_id=i, tile=(64, 16), graph=0))
+            out.append(w)
+        return out
+    wa, wb = worlds(), worlds()
+    ba, bb = H.Batch(wa), H.Batch(wb)
+    bad = ctypes.c_uint64()
+    for _ in range(3):
+        for w in wb:
+            H.check(H.lib.hg_world_poison_scratch(w.h))
+        bb.step(1, H.MODE_FUSED)
+        bb.sync()
+        for w in wb:
+            H.check(H.lib.hg_world_count_nonfinite(w.h, ctypes.byref(bad)))
+            assert bad.value == 0
+    ba.step(3, H.MODE_FUSED)
+    ba.sync()
+    assert bb.tuning()[0] == 0  # never tuned: the table launch ran
+    for x, y in zip(wa, wb):
+        for f in ("rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b"):
+            assert np.array_equal(x.download(f), y.download(f)), (x.n, f)
+    ba.close()
+    bb.close()
