@@ -22,13 +22,23 @@ slabs and `halo_max`, else every rank gathers the whole field (all-gather):
 the fallback the unbounded reach needs.  Halos come from the two neighbours
 only; no other data moves.
 
+`deep_block` trades the per-pass exchanges for one exchange every T steps:
+each rank receives D rows of the state from each neighbour, D the sum of
+the read radii of the block's passes (the sediment pass counted at a fixed
+back-trace budget), and every pass computes the rows that its inputs still
+determine, a range that shrinks by the pass's radius; the own rows come out
+as one world's.  Before each sediment pass the ranks agree on the largest
+back-trace reach over the rows it computes (all-reduce); above the budget,
+every rank restores its rows from the block's start and steps the block
+with the per-pass schedule instead.
+
 This module is the host-side schedule only.  It drives any `stepper` that
-runs one pass over the owned rows and reads and writes rows of a field
-(`run_pass`, `get_rows`, `set_rows`, `max_reach_rows`), through
-torch.distributed collectives on CPU tensors (gloo; a GPU stepper would pass
-device tensors to NCCL).  The tests drive it with the float oracle's passes
-restricted to a slab, bit for bit against one process stepping the whole
-world (tests/test_slabs_gloo.py).
+runs one pass over a row range and reads and writes rows of a field
+(`run_pass`, `set_compute_rows`, `get_rows`, `set_rows`, `max_reach_rows`,
+`set_step`), through torch.distributed collectives on CPU tensors (gloo; a
+GPU stepper would pass device tensors to NCCL).  The tests drive it with the
+float oracle's passes restricted to rows, bit for bit against one process
+stepping the whole world (tests/test_slabs_gloo.py).
 """
 import numpy as np
 
@@ -44,6 +54,13 @@ STEP_PLAN = [
     ("thermal_transport", 1, [("thc", 1), ("thd", 1)]),
     ("smoothing", 0, [("height", 1)]),
 ]
+
+
+# rows a pass reads around the rows it writes (the sediment pass: its
+# back-trace reach, bounded per block by the caller's budget)
+PASS_RADIUS = {"rain": 0, "flux": 1, "erosion": 1, "thermal_flux": 1, "thermal_transport": 1, "smoothing": 1}
+# the carried state (the thermal outflows are rewritten before every read)
+STATE_TEXTURES = ("height", "flux", "vel", "sed")
 
 
 def slab_rows(n, nranks):
@@ -87,6 +104,8 @@ class SlabComm:
         self.min_rows = min(hi - lo for lo, hi in rows)
         self.gathers = 0
         self.exchanges = 0
+        self.deep_blocks = 0  # blocks of steps after one exchange
+        self.rollbacks = 0    # blocks redone pass by pass (a back-trace beyond the budget)
 
     def agree_max(self, value):
         t = self.torch.tensor([float(value)], dtype=self.torch.float64)
@@ -128,6 +147,9 @@ class SlabComm:
 
 def slab_step(stepper, comm, step1, settings, rain_period, halo_max=8, rain_on=True):
     """One step of the owned rows: each pass after the halos it reads."""
+    lo, hi = comm.rows[comm.rank]
+    stepper.set_step(step1 - 1)
+    stepper.set_compute_rows(lo, hi)
     for name, layer, halos in passes_of_step(step1, settings, rain_period, rain_on):
         for field, depth in halos:
             if depth == "reach":
@@ -140,3 +162,58 @@ def slab_step(stepper, comm, step1, settings, rain_period, halo_max=8, rain_on=T
             else:
                 comm.exchange(stepper, field, depth)
         stepper.run_pass(name, layer)
+
+
+def block_depth(plans, sed_budget):
+    """Halo rows a block of steps needs: the read radii of its passes."""
+    return sum(sed_budget if name == "sediment" else PASS_RADIUS[name] for plan in plans for name, _, _ in plan)
+
+
+def deep_block(stepper, comm, step1, nsteps, settings, rain_period, sed_budget=2, halo_max=8, rain_on=True):
+    """Steps step1 .. step1 + nsteps - 1 of the owned rows after one halo
+    exchange (as many steps per exchange as the smallest slab allows, at
+    least one); returns the number of steps done.  A back-trace beyond
+    `sed_budget` rows sends every rank back to the block's start and through
+    slab_step (per-pass exchanges, `halo_max` as there)."""
+    lo, hi = comm.rows[comm.rank]
+    n = comm.n
+    plans = []
+    for k in range(nsteps):
+        p = passes_of_step(step1 + k, settings, rain_period, rain_on)
+        if block_depth(plans + [p], sed_budget) > comm.min_rows:
+            break
+        plans.append(p)
+    if not plans:  # not even one step's halo fits a slab
+        slab_step(stepper, comm, step1, settings, rain_period, halo_max, rain_on)
+        return 1
+    depth = block_depth(plans, sed_budget)
+    saved = {f: stepper.get_rows(f, lo, hi) for f in STATE_TEXTURES}
+    for f in STATE_TEXTURES:
+        comm.exchange(stepper, f, depth)
+    a, b = max(0, lo - depth), min(n, hi + depth)  # rows whose inputs are known
+
+    def shrink(r):  # the grid's own edges need no rows beyond them
+        return (a if a == 0 else a + r), (b if b == n else b - r)
+
+    for k, plan in enumerate(plans):
+        stepper.set_step(step1 + k - 1)
+        for name, layer, _ in plan:
+            if name == "sediment":
+                na, nb = shrink(sed_budget)
+                reach = int(comm.agree_max(stepper.max_reach_rows(na, nb)))
+                if reach > sed_budget:  # every rank sees the same maximum
+                    for f, rows in saved.items():
+                        stepper.set_rows(f, lo, rows)
+                    comm.rollbacks += 1
+                    for j in range(len(plans)):
+                        slab_step(stepper, comm, step1 + j, settings, rain_period, halo_max, rain_on)
+                    return len(plans)
+            else:
+                na, nb = shrink(PASS_RADIUS[name])
+            a, b = na, nb
+            stepper.set_compute_rows(a, b)
+            stepper.run_pass(name, layer)
+    assert a <= lo and b >= hi
+    stepper.set_compute_rows(lo, hi)
+    comm.deep_blocks += 1
+    return len(plans)

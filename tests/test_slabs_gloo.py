@@ -1,10 +1,14 @@
-"""One world split into row slabs over two gloo ranks on CPU (slabs.py).
+"""One world split into row slabs over gloo ranks on CPU (slabs.py).
 
-Each rank runs the float oracle's passes on its own rows only and gets the
-rows around them from its neighbour before each pass that reads them; the
-eroded sediment's halo follows the back-trace reach, with an all-gather when
-the reach leaves the halo.  After the steps every rank's rows equal one
-process stepping the whole world, bit for bit, and both sediment paths ran.
+Per-pass schedule: each rank runs the float oracle's passes on its own rows
+only and gets the rows around them from its neighbours before each pass
+that reads them; the eroded sediment's halo follows the back-trace reach,
+with an all-gather when the reach leaves the halo.  Deep-halo schedule: one
+exchange of the state's halo per block of steps, the passes computing a
+shrinking range of rows, and a roll-back to the per-pass schedule when a
+back-trace leaves the block's budget.  After the steps every rank's rows
+equal one process stepping the whole world, bit for bit, and each schedule's
+paths ran.
 """
 import os
 import socket
@@ -47,18 +51,26 @@ class OracleSlab:
     def run_pass(self, name, layer):
         self.w.run_pass(name, self.s, self.o, layer)
 
+    def set_compute_rows(self, a, b):
+        self.w.set_rows(a, b)
+
+    def set_step(self, done):
+        self.w.step_count = done
+
     def get_rows(self, field, y0, y1):
         return self.w.tex_rows(field, y0, y1)
 
     def set_rows(self, field, y0, rows):
         self.w.set_tex_rows(field, y0, rows)
 
-    def max_reach_rows(self):
-        v = self.w.tex_rows("vel", self.lo, self.hi)[..., 1]
+    def max_reach_rows(self, y0=None, y1=None):
+        y0 = self.lo if y0 is None else y0
+        y1 = self.hi if y1 is None else y1
+        v = self.w.tex_rows("vel", y0, y1)[..., 1]
         return int(np.ceil(np.max(np.abs(v)) * self.dt)) + 1 if v.size else 0
 
 
-def rank_main(rank, nranks, port, halo_max, films, out):
+def rank_main(rank, nranks, port, halo_max, films, out, deep=0):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(nranks))
     sys.path.insert(0, os.path.join(ROOT, "hydro-gen_gb300"))
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -70,22 +82,27 @@ def rank_main(rank, nranks, port, halo_max, films, out):
     s, o = workload(O, films)
     st = OracleSlab(O, rows, rank, s, o, s.d_t)
     comm = slabs.SlabComm(dist, rank, nranks, rows, N)
-    for k in range(STEPS):
+    k = 0
+    while k < STEPS:
+        if deep:
+            k += slabs.deep_block(st, comm, k + 1, min(deep, STEPS - k), s, o.rain_period, sed_budget=3,
+                                  halo_max=halo_max)
+        else:
+            slabs.slab_step(st, comm, k + 1, s, o.rain_period, halo_max=halo_max)
+            k += 1
         st.w.step_count = k
-        slabs.slab_step(st, comm, k + 1, s, o.rain_period, halo_max=halo_max)
-        st.w.step_count = k + 1
     lo, hi = rows[rank]
     mine = {f: st.w.get(f)[lo:hi] for f in FIELDS}
     dist.destroy_process_group()
-    out.put((rank, lo, hi, mine, comm.exchanges, comm.gathers))
+    out.put((rank, lo, hi, mine, comm.exchanges, comm.gathers, comm.deep_blocks, comm.rollbacks))
 
 
-def run_ranks(nranks, halo_max, films):
+def run_ranks(nranks, halo_max, films, deep=0):
     import torch.multiprocessing as mp
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = free_port()
-    procs = [ctx.Process(target=rank_main, args=(r, nranks, port, halo_max, films, q)) for r in range(nranks)]
+    procs = [ctx.Process(target=rank_main, args=(r, nranks, port, halo_max, films, q, deep)) for r in range(nranks)]
     for p in procs:
         p.start()
     res = [q.get(timeout=300) for _ in procs]
@@ -104,26 +121,47 @@ def test_slab_rows():
         slabs.slab_rows(4, 5)
 
 
-@pytest.mark.parametrize("films", [True, False])
-def test_two_ranks_equal_one_world(films):
+def one_world(films):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    res = run_ranks(2, 8, films)
     s, o = workload(O, films)
     w = O.OracleWorld(N, 32)
     w.set("rock", O.fbm(N, seed=1, frequency=1.0 / 16))
     w.step(s, o, STEPS)
-    exchanges = gathers = 0
+    return w
+
+
+def check_equal(res, w):
+    """Every rank's rows equal the one world's; the ranks' counters summed."""
     covered = np.zeros(N, bool)
-    for rank, lo, hi, mine, ex, ga in res:
-        exchanges, gathers = exchanges + ex, gathers + ga
+    tot = np.zeros(4, int)
+    for rank, lo, hi, mine, *counters in res:
+        tot += np.array(counters)
         covered[lo:hi] = True
         for f in FIELDS:
-            ref = w.get(f)[lo:hi]
-            bad = np.argwhere(mine[f] != ref)
+            bad = np.argwhere(mine[f] != w.get(f)[lo:hi])
             assert bad.size == 0, f"rank {rank} {f}: {len(bad)} cells differ"
     assert covered.all()
+    return tot  # exchanges, gathers, deep blocks, roll-backs
+
+
+@pytest.mark.parametrize("films", [True, False])
+def test_two_ranks_equal_one_world(films):
+    exchanges, gathers, _, _ = check_equal(run_ranks(2, 8, films), one_world(films))
     assert exchanges > 0
     # thin films send back-traces past the halo (the all-gather ran); with
     # uniform rain every step's sediment halo was a neighbour exchange
     assert (gathers > 0) == films
+
+
+@pytest.mark.parametrize("nranks,films", [(2, False), (2, True), (3, False)])
+def test_deep_halo_blocks_equal_one_world(nranks, films):
+    """Blocks of up to 4 steps per exchange (10 halo rows a step at a
+    back-trace budget of 3 rows, the uniform-rain workload's largest reach:
+    two steps on 24-row slabs, one on 16-row ones)."""
+    exchanges, gathers, deep_blocks, rollbacks = check_equal(run_ranks(nranks, 8, films, deep=4), one_world(films))
+    assert exchanges > 0
+    if films:  # thin-film back-traces overrun the budget: blocks redone pass by pass
+        assert rollbacks > 0 and gathers > 0
+    else:  # uniform rain: every block completed after its one exchange
+        assert deep_blocks > 0 and rollbacks == 0 and gathers == 0
