@@ -113,20 +113,23 @@ class SlabComm:
         return float(t.item())
 
     def exchange(self, stepper, field, depth):
-        """Refresh `depth` rows on each side of the own slab from the
-        neighbours (depth <= the smallest slab)."""
-        torch = self.torch
+        """Refresh `depth` rows on each side of the own slab from the two
+        neighbours (depth <= the smallest slab): point-to-point, one block
+        each way per neighbour, nothing to the other ranks."""
+        torch, dist = self.torch, self.dist
         lo, hi = self.rows[self.rank]
-        blk = np.zeros((2, depth, self.n, self.ch))
-        blk[0] = stepper.get_rows(field, lo, lo + depth)  # to the rank below
-        blk[1] = stepper.get_rows(field, hi - depth, hi)  # to the rank above
-        mine = torch.from_numpy(blk)
-        allb = [torch.empty_like(mine) for _ in range(self.nranks)]
-        self.dist.all_gather(allb, mine)
-        if self.rank > 0:  # rows [lo - depth, lo): the top rows of rank - 1
-            stepper.set_rows(field, lo - depth, allb[self.rank - 1][1].numpy())
-        if self.rank < self.nranks - 1:  # rows [hi, hi + depth): the bottom rows of rank + 1
-            stepper.set_rows(field, hi, allb[self.rank + 1][0].numpy())
+        reqs, recv = [], []
+        for nb, send_rows, recv_at in ((self.rank - 1, (lo, lo + depth), lo - depth),
+                                       (self.rank + 1, (hi - depth, hi), hi)):
+            if 0 <= nb < self.nranks:
+                out = torch.from_numpy(np.ascontiguousarray(stepper.get_rows(field, *send_rows)))
+                inc = torch.empty_like(out)
+                reqs += [dist.isend(out, nb), dist.irecv(inc, nb)]
+                recv.append((recv_at, inc))
+        for r in reqs:
+            r.wait()
+        for at, inc in recv:
+            stepper.set_rows(field, at, inc.numpy())
         self.exchanges += 1
 
     def gather(self, stepper, field):
