@@ -1862,6 +1862,14 @@ int hg_tape_info(const hg_tape* t, int* nsteps, int* ckpt_every) {
     return HG_OK;
 }
 
+// Segments: the first holds the remainder, nsteps - (nseg - 1) K steps (1 to
+// K), every later one K steps, so the last segment, which the forward leaves
+// in the segment buffers, is a whole interval and the backward recomputes
+// nsteps - K steps.
+int seg_len(const hg_tape* t, int s) { return s == 0 ? t->nsteps - (t->nseg - 1) * t->K : t->K; }
+// Steps before segment s (relative to the tape's first step).
+uint64_t seg_start(const hg_tape* t, int s) { return s == 0 ? 0 : (uint64_t)seg_len(t, 0) + (uint64_t)(s - 1) * t->K; }
+
 // Segment buffer b: its K states and K slot groups.
 float* seg_buf(hg_tape* t, int b) { return t->seg + (size_t)b * t->K * kStateFields * cells(t->w); }
 float* slot_buf(hg_tape* t, int b) { return t->slots + (size_t)b * t->K * kSlotFields * cells(t->w); }
@@ -1877,7 +1885,7 @@ int recompute_segment(hg_tape* t, int s, int len, const StepConsts& cst, int th,
     const size_t c = cells(w), sf = kStateFields * c;
     float* segb = seg_buf(t, b);
     float* slotb = slot_buf(t, b);
-    k_set_u64<<<1, 1, 0, st>>>(t->d_step, (unsigned long long)(t->step0 + (uint64_t)s * t->K));
+    k_set_u64<<<1, 1, 0, st>>>(t->d_step, (unsigned long long)(t->step0 + seg_start(t, s)));
     TerrainSrc src{};
     src.c = cst;
     src.rain = make_rain_base(w);
@@ -1916,7 +1924,7 @@ int hg_forward(hg_tape* t) {
     for (int s = 0; s < t->nseg; ++s) {
         int rc = copy_state_out(w, t->ckpt + (size_t)s * kStateFields * c, w->stream);
         if (rc != HG_OK) return rc;
-        const int len = std::min(t->K, t->nsteps - s * t->K);
+        const int len = seg_len(t, s);
         if (s + 1 < t->nseg) {
             rc = hg_step(w, len, HG_MODE_FUSED);
             if (rc != HG_OK) return rc;
@@ -1991,7 +1999,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     auto recompute = [&](int s, cudaStream_t rs) -> int {
         const int b = buf_of(s);
         if (overlap) HG_CUDA(cudaStreamWaitEvent(rs, t->ev_rev[b], 0));  // the sweep that used b is done
-        int rc = recompute_segment(t, s, std::min(t->K, t->nsteps - s * t->K), cst, th, nullptr, b, rs);
+        int rc = recompute_segment(t, s, seg_len(t, s), cst, th, nullptr, b, rs);
         if (rc != HG_OK) return rc;
         if (overlap) HG_CUDA(cudaEventRecord(t->ev_rec[b], rs));
         return HG_OK;
@@ -2013,7 +2021,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
     int cur = 0;      // buffer holding the adjoint of the next reversed step's output
     uint64_t m = 0;   // reversed steps so far: step m uses dse[m & 1]
     for (int s = t->nseg - 1; s >= 0; --s) {
-        const int len = std::min(t->K, t->nsteps - s * t->K);
+        const int len = seg_len(t, s);
         bcur = buf_of(s);
         if (overlap) {
             HG_CUDA(cudaStreamWaitEvent(st, t->ev_rec[bcur], 0));
@@ -2032,7 +2040,7 @@ int hg_backward(hg_tape* t, const float* dL_drock_final, float* dL_dks, float* d
             for (int f = 0; f < kStateFields; ++f)
                 if (!t->tma.get(xin + f * c, w->n, adjoint_box_rows(), &args.maps[f]))
                     return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a tape buffer");
-            args.rain = make_rain(w, t->step0 + (uint64_t)s * t->K + j + 1);
+            args.rain = make_rain(w, t->step0 + seg_start(t, s) + j + 1);
             args.A = view(cur);
             args.dse = dse[m & 1];
             args.dse_prev = dse[(m + 1) & 1];

@@ -105,6 +105,43 @@ def test_checkpoint_interval_does_not_change_gradients():
         assert rel_l2(db0, outs[0][2]) <= 1e-5
 
 
+def test_ragged_segments_under_step_keyed_rain():
+    """Bernoulli rain is keyed on the step number, so every segment's steps
+    must take their own numbers in the forward, the recompute and the
+    reverse.  With checkpoint intervals that leave a short first segment
+    (29 = 3 + 2 x 13 = 1 + 4 x 7) the gradients equal those of the whole
+    tape in memory (interval 29, nothing recomputed) up to the order of the
+    sediment adjoint's atomic adds, and the forward's final state equals 29
+    plain fused steps bit for bit."""
+    n, nsteps = 128, 29
+    torch_dev()
+
+    def world():
+        w = H.World(n)
+        w.init_heightmap(H.noise(seed=1, frequency=1.0 / 32))
+        H.configure(w, "config2")
+        w.set_options(H.options(H.RAIN_BERNOULLI, p=0.05, seed=5))
+        w.init_ks_field(H.noise(seed=7, octaves=3, frequency=1.0 / 64), 0.05, 0.5)
+        return w
+
+    ref = world()
+    ref.step(nsteps, H.MODE_FUSED)
+    final = {f: ref.download(f) for f in H.STATE_FIELDS}
+    target = world().download("rock") * 0.999
+    outs = {}
+    for ckpt in (29, 13, 7):
+        w = world()
+        outs[ckpt] = gpu_gradients(w, target, nsteps, ckpt)
+        assert outs[ckpt][3].ckpt_every == ckpt
+        for f in H.STATE_FIELDS:
+            assert np.array_equal(w.download(f), final[f]), (ckpt, f)
+    loss, dks, db0, _ = outs[29]
+    assert np.abs(dks).max() > 0
+    for ckpt in (13, 7):
+        assert outs[ckpt][0] == loss
+        assert rel_l2(outs[ckpt][1], dks) <= 1e-5 and rel_l2(outs[ckpt][2], db0) <= 1e-5, ckpt
+
+
 @pytest.mark.parametrize("thermal", [False, True])
 def test_tape_forward_is_the_fused_step(thermal):
     a = make_world(128, thermal=thermal)
