@@ -1015,16 +1015,16 @@ def main():
     value = job_throughput(world_size, cells, args.steps, fused_ms / 1e3)
     plain_value = job_throughput(world_size, cells, plain_steps, plain_ms / 1e3)
 
-    # e2e: C ABI with pinned host buffers, copies inside the timed region
-    host = {f: torch.zeros((n, n), dtype=torch.float32).pin_memory() for f in H.STATE_FIELDS[:7]}
-    host["rock"].copy_(torch.from_numpy(init["rock"]))
+    # e2e: C ABI with pinned host buffers, copies inside the timed region.
+    # The workload's input is its initial heightmap (water, sediment and
+    # flux start at zero, set on the device as the reference's texture
+    # creation does); its result is read back as rock, water and sediment.
+    rock_host = torch.from_numpy(init["rock"]).pin_memory()
     outs = {f: torch.empty((n, n), dtype=torch.float32).pin_memory() for f in ("rock", "water", "sediment")}
     barrier()
     t0 = time.perf_counter()
-    for f, t in host.items():
-        H.check(H.lib.hg_world_upload(w.h, H.FIELDS[f], t.data_ptr()))
-    t1 = time.perf_counter()  # the uploads return once their copies are done
-    w.step_count = 0
+    H.check(H.lib.hg_init_heightmap_host(w.h, H.ctypes.c_void_p(rock_host.data_ptr())))
+    t1 = time.perf_counter()  # returns once its copy is done
     w.step(args.steps, H.MODE_FUSED)
     w.sync()
     t2 = time.perf_counter()
@@ -1033,11 +1033,12 @@ def main():
     barrier()
     t3 = time.perf_counter()
     e2e_s = max_over_ranks(dist, t3 - t0, "cuda")
-    h2d = 7 * cells * 4 / args.steps
+    h2d = cells * 4 / args.steps
     d2h = 3 * cells * 4 / args.steps
     # the copies' own rates from pinned memory (the host link bounds them:
-    # about 210 GB/s up and 190 GB/s down on GB300, whatever the copy form)
-    copy_rates = {"h2d_gbs": 7 * cells * 4 / (t1 - t0) / 1e9, "d2h_gbs": 3 * cells * 4 / (t3 - t2) / 1e9}
+    # about 210 GB/s up and 190 GB/s down on GB300, whatever the copy form;
+    # the upload's time includes zeroing the other fields on the device)
+    copy_rates = {"h2d_gbs": cells * 4 / (t1 - t0) / 1e9, "d2h_gbs": 3 * cells * 4 / (t3 - t2) / 1e9}
     # the ragged batch split over the ranks: every rank takes part, rank 0 reports
     sharded = None
     if world_size > 1 and not args.no_extras:

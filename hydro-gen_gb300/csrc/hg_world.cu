@@ -1187,6 +1187,21 @@ int hg_init_heightmap(hg_world* w, const hg_noise_settings* s) {
     return HG_OK;
 }
 
+int hg_init_heightmap_host(hg_world* w, const float* rock) {
+    Range nv_range("hg_init_heightmap_host");
+    HG_CHECK_WORLD(w);
+    if (!rock) return fail(HG_ERR_INVALID, "null heightmap");
+    DeviceGuard g(w->device);
+    int rc = zero_state(w);
+    if (rc != HG_OK) return rc;
+    HG_CUDA(cudaMemcpyAsync(w->cur[S_ROCK], rock, cells(w) * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    w->step = 0;
+    w->dev_step_valid = false;
+    w->invalid = false;
+    return HG_OK;
+}
+
 int hg_world_count_nonfinite(hg_world* w, uint64_t* count) {
     HG_CHECK_WORLD(w);
     if (!count) return fail(HG_ERR_INVALID, "null output");

@@ -121,6 +121,7 @@ def _load():
         "hg_set_rain_settings": (ctypes.c_int, [P, ctypes.POINTER(RainSettings)]),
         "hg_set_step_options": (ctypes.c_int, [P, ctypes.POINTER(StepOptions)]),
         "hg_init_heightmap": (ctypes.c_int, [P, ctypes.POINTER(NoiseSettings)]),
+        "hg_init_heightmap_host": (ctypes.c_int, [P, P]),
         "hg_init_ks_field": (ctypes.c_int, [P, ctypes.POINTER(NoiseSettings), ctypes.c_float, ctypes.c_float]),
         "hg_clear_ks_field": (ctypes.c_int, [P]),
         "hg_world_upload": (ctypes.c_int, [P, ctypes.c_int, P]),
@@ -356,6 +357,16 @@ class World:
 
     def init_heightmap(self, ns):
         check(lib.hg_init_heightmap(self.h, ctypes.byref(ns)))
+
+    def init_from_heightmap(self, rock):
+        """Every field zero, ROCK from a host heightmap (n x n float32 array or
+        a pointer to n*n floats, pinned for the fastest copy), step 0."""
+        if isinstance(rock, int):
+            check(lib.hg_init_heightmap_host(self.h, ctypes.c_void_p(rock)))
+            return
+        a = np.ascontiguousarray(rock, dtype=np.float32)
+        assert a.size == self.n * self.n
+        check(lib.hg_init_heightmap_host(self.h, ctypes.c_void_p(a.ctypes.data)))
 
     def init_reference_heightmap(self, ms):
         """The reference's terrain generator (glsl/heightmap.glsl)."""

@@ -303,6 +303,14 @@ int hg_init_ks_field(hg_world* w, const hg_noise_settings* s, float base, float 
 /* Drops the per-cell solubility field (Ks[0] applies again). */
 int hg_clear_ks_field(hg_world* w);
 
+/* Starts the world from a caller's heightmap: every field to zero on the
+ * device (dirt too in two-layer worlds; the per-cell Ks field stays), then
+ * ROCK from caller-owned host memory (n*n floats), step counter 0; the
+ * counterpart of creating zero-filled textures (State::World::gen_textures,
+ * src/state.cpp:3-44) and writing the heightmap into them.  Synchronous with
+ * respect to the host.  HG_ERR_INVALID for a null heightmap. */
+int hg_init_heightmap_host(hg_world* w, const float* rock);
+
 /* Copy one field between caller-owned host memory (n*n floats) and the world.
  * Synchronous with respect to the host.  Uploading ROCK or WATER is the
  * equivalent of writing the heightmap texture. */

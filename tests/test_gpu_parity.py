@@ -276,3 +276,29 @@ def test_paired_arithmetic_is_scalar_arithmetic():
     bad = (ctypes.c_uint64 * 6)()
     H.check(H.lib.hg_selftest_paired(777, 1 << 26, bad))
     assert list(bad) == [0, 0, 0, 0, 0, 0], list(bad)
+
+
+def test_init_from_host_heightmap_is_a_fresh_world():
+    """hg_init_heightmap_host on a world that has stepped (every field
+    non-zero) gives the fields and steps of a fresh world initialised on the
+    device: zeros everywhere, the host heightmap as rock, step 0 (the next
+    step's Bernoulli rain is step 1's)."""
+    n = 192
+    fresh = H.World(n)
+    fresh.init_heightmap(H.noise(seed=4))
+    H.configure(fresh, "config2")
+    rock = fresh.download("rock")
+    used = H.World(n)
+    used.init_heightmap(H.noise(seed=9))
+    H.configure(used, "config2")
+    used.step(7, H.MODE_FUSED)
+    used.init_from_heightmap(rock)
+    assert used.step_count == 0
+    for f in H.STATE_FIELDS:
+        assert np.array_equal(used.download(f), fresh.download(f)), f
+    fresh.step(12, H.MODE_FUSED)
+    used.step(12, H.MODE_FUSED)
+    for f in H.STATE_FIELDS:
+        assert np.array_equal(used.download(f), fresh.download(f)), f
+    import ctypes
+    assert H.lib.hg_init_heightmap_host(used.h, ctypes.c_void_p(0)) == -1  # HG_ERR_INVALID
