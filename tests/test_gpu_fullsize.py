@@ -1,4 +1,4 @@
-"""Full-size workloads (4096², 8192²).
+"""Full-size workloads (4096², 8192², 16384²).
 
 The headline workload (4096², Bernoulli rain p = 0.001, talus slippage) is
 compared bit for bit with the float oracle on every state field after 20
@@ -90,6 +90,19 @@ def test_large_8192_thermal_fused_equals_plain():
         w.set_options(H.options(H.RAIN_UNIFORM))
         return w
     run_pair(make, 4, ONE)
+
+
+def test_largest_16384_fused_equals_plain():
+    """The largest size the tests step: 16384² (268 M cells, 2^28, about
+    35 GB of fields and scratch per world; the cell index is 64-bit and a
+    launch has 262,144 tiles), the metric's physics and rain."""
+    def make():
+        w = H.World(16384)
+        w.init_heightmap(H.noise(seed=0))
+        H.configure(w, "config2")
+        return w
+    f = run_pair(make, 3, ONE)
+    assert float(f["water"].max()) > 0.0 and float(f["sediment"].abs().max()) > 0.0
 
 
 def test_two_layer_4096_reference_defaults_fused_equals_plain():
