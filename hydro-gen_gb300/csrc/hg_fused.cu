@@ -108,6 +108,31 @@ __device__ __forceinline__ RainStep rain_for(const RainBase& rb, unsigned long l
 // ---------------------------------------------------------------------------
 // k_hydro
 // ---------------------------------------------------------------------------
+// Sets the cells of a staged box that lie outside the grid to v.  The box
+// (ROWS x RW cells, row 0 at global row gy0, column 0 at global column
+// gx0 = tx0 - HX) reaches past the grid only through its HX outer columns
+// on either side and its HALO outer rows on either side, so only those
+// are visited (a corner cell twice, with the same value).
+template <int ROWS, int HALO, int NTH>
+__device__ __forceinline__ void fill_outside(float* box, int gx0, int gy0, int n, float v, int tid) {
+    constexpr int SIDE = ROWS * 2 * HX;  // the outer columns of every row
+    constexpr int CAP = 2 * HALO * RW;   // the outer rows
+    for (int i = tid; i < SIDE + CAP; i += NTH) {
+        int r, col;
+        if (i < SIDE) {
+            r = i / (2 * HX);
+            const int k = i % (2 * HX);
+            col = k < HX ? k : RW - 2 * HX + k;
+        } else {
+            const int j = i - SIDE, rr = j / RW;
+            col = j % RW;
+            r = rr < HALO ? rr : ROWS - 2 * HALO + rr;
+        }
+        const int gx = gx0 + col, gy = gy0 + r;
+        if (gx < 0 || gx >= n || gy < 0 || gy >= n) box[r * RW + col] = v;
+    }
+}
+
 // EM: 0 inner tile, 1 edge tile (each its own code), 2 either, told at run
 // time by edge_rt (one code path for both)
 template <int TH, int EM>
@@ -167,11 +192,7 @@ __device__ __forceinline__ void hydro_tile(const TerrainHot& td, const CUtensorM
                  // out-of-range height: with rock 0 there, the neighbour's total height
                  // rock + water is exactly FAR_HEIGHT; rock 0 and flux 0 outside are
                  // what the shader reads there too, so neighbour reads need no test
-        float* Dw = sm + H_D * H_RC;
-        for (int i = tid; i < G::H_BOX; i += NTH) {
-            const int gx = gx0 + i % RW, gy = gy0 + i / RW;
-            if (gx < 0 || gx >= n || gy < 0 || gy >= n) Dw[i] = FAR_HEIGHT;
-        }
+        fill_outside<H_RH, 1, NTH>(sm + H_D * H_RC, gx0, gy0, n, FAR_HEIGHT, tid);
     }
     __syncthreads();
 
@@ -408,10 +429,7 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
     }
     if (EDGE) {  // the box's cells outside the grid (zero-filled by the copy) become the
                  // shader's out-of-range height, so every neighbour read needs no test
-        for (int i = tid; i < G::T_BOX; i += G::NTH) {
-            const int gx = gx0 + i % RW, gy = gy0 + i / RW;
-            if (gx < 0 || gx >= n || gy < 0 || gy >= n) be[i] = FAR_HEIGHT;
-        }
+        fill_outside<G::T_RH, 2, G::NTH>(be, gx0, gy0, n, FAR_HEIGHT, tid);
         __syncthreads();
     }
     // the taps' loads were issued with the tile's copy: mix them now, before
