@@ -391,12 +391,14 @@ int hg_world_totals(hg_world* w, double out[3]);
 /* No counterpart in the reference.  Reverse-mode adjoint of the one-layer
  * step (rain, flux, erosion, sediment transport and, when on, the talus
  * passes; not smoothing), for fitting the per-cell rock solubility and the
- * initial rock heights.  A tape records nsteps steps of w with a checkpoint
- * of the carried fields every ckpt_every steps (HG_AUTO: the longest
- * interval whose tape fits in the free device memory less a reserve of a
- * tenth of it, at least 4 GiB; up to nsteps, when nothing is recomputed);
- * hg_backward recomputes each segment but the last from its checkpoint and
- * runs the reverse kernels.  Subgradients at max/min/clamp and at the
+ * initial rock heights.  A tape records nsteps steps of w in segments: the
+ * first of nsteps - (nseg - 1) * ckpt_every steps, the others of ckpt_every
+ * (HG_AUTO: the longest interval whose tape fits in the free device memory
+ * less a reserve of a tenth of it, at least 4 GiB; up to nsteps, when
+ * nothing is recomputed), with a checkpoint of the carried fields at each
+ * segment's start; the last segment stays in the tape, and hg_backward
+ * recomputes the others from their checkpoints (nsteps - ckpt_every steps)
+ * and runs the reverse kernels.  Subgradients at max/min/clamp and at the
  * dissolve/deposit branches: the taken branch's derivative.  The world's
  * settings and per-cell Ks must not change between hg_forward and
  * hg_backward.  Destroying a world frees the device memory of its live
