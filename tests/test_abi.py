@@ -72,6 +72,16 @@ def test_error_paths_without_a_device(hg):
     assert hg.lib.hg_default_fit_settings(ctypes.byref(fs)) == 0
     assert (fs.nsteps, fs.ckpt_every, fs.iters) == (256, 32, 8)
     assert hg.lib.hg_inverse_fit(None, None, None, None, ctypes.byref(fs), None, None) == -1
+    assert hg.lib.hg_init_heightmap_host(None, None) == -1
+    # the allocation-free totals check their arguments before any CUDA call
+    out = ctypes.c_void_p(1)
+    ptrs = (ctypes.c_void_p * 9)(*([1] * 9))
+    assert hg.lib.hg_field_totals_noalloc(None, 1, 16, out, None) == -1
+    assert hg.lib.hg_field_totals_noalloc(ptrs, 0, 16, out, None) == -1
+    assert hg.lib.hg_field_totals_noalloc(ptrs, 9, 16, out, None) == -1  # more than HG_NOALLOC_MAX_FIELDS
+    assert b"nfields" in hg.lib.hg_last_error()
+    nulls = (ctypes.c_void_p * 2)(1, None)
+    assert hg.lib.hg_field_totals_noalloc(nulls, 2, 16, out, None) == -1
 
 
 def test_log_callback_receives_failures(hg):
