@@ -157,16 +157,18 @@ struct Plan {
     std::vector<float*> smooth_dst[2];  // per direction and world: the step's rock output when smoothing runs
                                         // (the fused kernels then leave their rock in the world's scratch)
     std::vector<uint64_t> versions;
-    cudaGraphExec_t graph[2] = {};  // two steps starting with table 0 / table 1
-    uint64_t graph_launches = 4;    // kernel launches in one graph
+    // captured steps starting with table 0 / table 1: [0] two steps, [1] kLongGraph
+    cudaGraphExec_t graph[2][2] = {};
+    uint64_t graph_launches[2] = {4, 4};  // kernel launches in one replay of each
     cudaStream_t stream = nullptr;
     int* err = nullptr;
 };
 
 void destroy_plan(Plan*& p) {
     if (!p) return;
-    for (auto& g : p->graph)
-        if (g) cudaGraphExecDestroy(g);
+    for (auto& gl : p->graph)
+        for (auto& g : gl)
+            if (g) cudaGraphExecDestroy(g);
     for (int d = 0; d < 2; ++d) {
         cudaFree(p->d_maps[d]);
         delete p->bp[d];
@@ -422,12 +424,13 @@ void rain_pass(hg_world* w, const StepConsts& c, uint64_t step1, const float* ro
 // (table 0 steps cur -> alt, table 1 alt -> cur) and records the build state.
 int build_plan(Plan* p) {
     const size_t nt = p->worlds.size();
-    for (auto& g : p->graph)  // captured launches hold the old descriptors
-        if (g) {
-            cudaStreamSynchronize(p->stream);
-            cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
+    for (auto& gl : p->graph)  // captured launches hold the old descriptors
+        for (auto& g : gl)
+            if (g) {
+                cudaStreamSynchronize(p->stream);
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
     std::vector<int> tile0(nt);
     p->total = 0;
     for (size_t i = 0; i < nt; ++i) {
@@ -528,6 +531,30 @@ void launch_dir(Plan* p, int dir) {
 // Brings a plan up to date (tables, device step counters, the graph that
 // starts with the next direction) without running a step; *dir gets the
 // next direction.
+// Steps per replay of a plan's long graph: graph launches cost the GPU a
+// few microseconds each, so long runs replay kLongGraph steps at a time
+// (an even count: the buffers are back in their roles after it).
+constexpr int kLongGraph = 8;
+
+// Captures (once) the graph of `which` (0: two steps, 1: kLongGraph steps)
+// starting with descriptor table `dir`.
+int capture_steps(Plan* p, int dir, int which) {
+    if (p->graph[which][dir]) return HG_OK;
+    const int steps = which ? kLongGraph : 2;
+    cudaGraph_t g = nullptr;
+    const uint64_t before = g_launches.load();
+    HG_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < steps; ++k) launch_dir(p, (dir + k) & 1);
+    cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+    p->graph_launches[which] = g_launches.load() - before;  // captured, not run
+    g_launches.fetch_sub(p->graph_launches[which]);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&p->graph[which][dir], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return HG_OK;
+}
+
 int prepare_plan(Plan* p, bool use_graph, int* dir_out) {
     int dir = plan_dir(p);
     if (dir < 0) {
@@ -540,21 +567,11 @@ int prepare_plan(Plan* p, bool use_graph, int* dir_out) {
             k_set_u64<<<1, 1, 0, p->stream>>>(w->d_step, (unsigned long long)w->step);
             w->dev_step_valid = true;
         }
-    const int nt = (int)p->worlds.size();
-    if (use_graph && !p->graph[dir]) {
-        cudaGraph_t g = nullptr;
-        const uint64_t before = g_launches.load();
-        HG_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
-        launch_dir(p, dir);
-        launch_dir(p, 1 - dir);
-        cudaError_t e = cudaStreamEndCapture(p->stream, &g);
-        p->graph_launches = g_launches.load() - before;  // captured, not run
-        g_launches.fetch_sub(p->graph_launches);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&p->graph[dir], g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
-    }
+    if (use_graph)  // both lengths up front: no capture inside a later call's steps
+        for (int which = 0; which < 2; ++which) {
+            int rc = capture_steps(p, dir, which);
+            if (rc != HG_OK) return rc;
+        }
     *dir_out = dir;
     return HG_OK;
 }
@@ -572,9 +589,13 @@ int run_plan(Plan* p, int nsteps, bool use_graph) {
     const int nt = (int)p->worlds.size();
     int k = 0;
     if (use_graph && nsteps >= 2) {
+        for (; k + kLongGraph <= nsteps; k += kLongGraph) {
+            HG_CUDA(cudaGraphLaunch(p->graph[1][dir], p->stream));
+            count_launch(p->graph_launches[1]);
+        }
         for (; k + 2 <= nsteps; k += 2) {
-            HG_CUDA(cudaGraphLaunch(p->graph[dir], p->stream));
-            count_launch(p->graph_launches);
+            HG_CUDA(cudaGraphLaunch(p->graph[0][dir], p->stream));
+            count_launch(p->graph_launches[0]);
         }
     }
     for (; k < nsteps; ++k) {
@@ -601,7 +622,8 @@ int run_plan(Plan* p, int nsteps, bool use_graph) {
 // Fused steps over `worlds` with the autotuned (or requested) variant.  The
 // first call with at least 8 steps and no tuned choice times two steps of
 // each variant (tile height 16/8 x direct launches/graph replay); every
-// variant gives identical fields, so tuning steps are ordinary steps.
+// variant gives identical fields, so tuning steps are ordinary steps.  Graph
+// replay runs kLongGraph steps per replay while that many remain, then two.
 int fused_run(Plan** plans, const std::vector<hg_world*>& worlds, Tuning& tune, int req_th, int req_graph,
               cudaStream_t st, int* err, int nsteps) {
     for (hg_world* w : worlds) {
