@@ -531,9 +531,9 @@ void launch_dir(Plan* p, int dir) {
 // Brings a plan up to date (tables, device step counters, the graph that
 // starts with the next direction) without running a step; *dir gets the
 // next direction.
-// Steps per replay of a plan's long graph: graph launches cost the GPU a
-// few microseconds each, so long runs replay kLongGraph steps at a time
-// (an even count: the buffers are back in their roles after it).
+// Steps per replay of a plan's long graph: long runs replay kLongGraph
+// steps at a time (an even count: the buffers are back in their roles
+// after it), a quarter of the host's graph launches.
 constexpr int kLongGraph = 8;
 
 // Captures (once) the graph of `which` (0: two steps, 1: kLongGraph steps)
