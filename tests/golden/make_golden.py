@@ -21,7 +21,11 @@ Workloads (seeded simplex fBm heightmaps, seed 0, scaled to [0, 64]):
 config1_256x100 (uniform rain 0.01, no thermal, 100 steps), config2_256x100
 (thermal, Bernoulli rain 0.5 at p = 0.001, 100 steps) and two_layer_128x40
 (rock + dirt, the reference's default settings of src/state.cpp:81-92,
-uniform rain 0.01, 40 steps).
+uniform rain 0.01, 40 steps); then particles_128x25 (4096 droplets on a
+two-layer 128² world with the reference's particle defaults, 25 steps:
+fields, momentum map and droplet state) and render_config2_256x100 (a
+96 x 96 frame of the ray-marcher over config2_256x100's final fields: the
+RGBA8 pixels and the float colours' bits).
 """
 import hashlib
 import json
@@ -107,16 +111,55 @@ def digest(a):
     return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float32).tobytes()).hexdigest()
 
 
+PARTICLES = {"n": 128, "count": 4096, "steps": 25, "rain_seed": 7, "rock_seed": 0, "dirt_seed": 3, "dirt_hi": 2.0}
+RENDER = {"of": "config2_256x100", "pos": [-10.0, 120.0, 96.0], "dir": [1.0, -0.7, 0.1], "aspect": 1.0,
+          "width": 96, "height": 96, "max_height": 256.0, "hmap_dim_x": 1024}
+DROPLETS = ["rock", "dirt", "water", "vel_u", "vel_v"]  # vel_u / vel_v: the momentum map's x / y
+
+
+def particle_run(O, H):
+    """The oracle's particle mode (droplets in id order) on PARTICLES."""
+    P = PARTICLES
+    s = H.settings_particles()
+    w = O.OracleWorld(P["n"], 32)
+    w.set("rock", O.fbm(P["n"], seed=P["rock_seed"]))
+    w.set("dirt", O.fbm(P["n"], seed=P["dirt_seed"], lo=0.0, hi=P["dirt_hi"]))
+    w.particles_init(P["count"])
+    o = O.options(1, 1, 0.0, seed=P["rain_seed"])
+    for _ in range(P["steps"]):
+        w.particle_step(O.erosion_from(s), o, 1)
+    return w
+
+
+def particle_digests(fields, state, iters, kill):
+    out = {f: digest(a) for f, a in fields.items()}
+    out["droplet_state"] = hashlib.sha256(np.ascontiguousarray(state, dtype=np.float32).tobytes()).hexdigest()
+    out["droplet_iters"] = hashlib.sha256(np.ascontiguousarray(iters, dtype=np.uint32).tobytes()).hexdigest()
+    out["droplet_kill"] = hashlib.sha256(np.ascontiguousarray(kill, dtype=np.int32).tobytes()).hexdigest()
+    return out
+
+
+def render_digests(rgba, rgb):
+    return {"rgba8": hashlib.sha256(np.ascontiguousarray(rgba, dtype=np.uint8).tobytes()).hexdigest(),
+            "rgb_bits": hashlib.sha256(np.ascontiguousarray(rgb, dtype=np.float32).view(np.uint32).tobytes()).hexdigest()}
+
+
+def render_camera(H):
+    return H.camera(tuple(RENDER["pos"]), tuple(RENDER["dir"]), aspect=RENDER["aspect"])
+
+
 def main():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "hydro-gen_gb300"))
     import oracle as O
+    import hydrogen as H
     golden, crops = {}, {}
     for name, (n, steps, layers, s, o) in cases(O).items():
         fields = TWO if layers == 2 else ONE
         w = run_oracle(O, n, steps, layers, s, o, 32)
         w64 = run_oracle(O, n, steps, layers, s, o, 64)
         t64 = w64.totals()  # rock, dirt, water, sediment (both channels)
-        entry = {"n": n, "steps": steps, "layers": layers, "init_seeds": {"rock": 0, "dirt": 3},
+        entry = {"kind": "grid", "n": n, "steps": steps, "layers": layers, "init_seeds": {"rock": 0, "dirt": 3},
                  "settings": settings_dict(s), "options": options_dict(o), "sha256": {}, "sum_f64": {},
                  "fp64_oracle_totals": {"rock": t64[0], "dirt": t64[1], "water": t64[2], "sediment": t64[3]}}
         for f in fields:
@@ -127,6 +170,17 @@ def main():
                 crops[f"{name}/{f}/{cname}"] = a[y:y + 8, x:x + 8].copy()
         golden[name] = entry
         print(name, {f: entry["sha256"][f][:12] for f in fields})
+        if name == RENDER["of"]:
+            rgba, rgb = O.render({f: w.get(f).astype(np.float32) for f in ("rock", "water", "sediment")}, n,
+                                 render_camera(H), RENDER["width"], RENDER["height"], RENDER["max_height"],
+                                 RENDER["hmap_dim_x"])
+            golden["render_" + name] = dict(RENDER, kind="render", sha256=render_digests(rgba, rgb))
+            print("render_" + name, golden["render_" + name]["sha256"])
+    pw = particle_run(O, H)
+    st, it, kl = pw.particles()
+    golden["particles_128x25"] = dict(PARTICLES, kind="particles", sha256=particle_digests(
+        {f: pw.get(f).astype(np.float32) for f in DROPLETS}, st, it, kl))
+    print("particles_128x25", {k: v[:12] for k, v in golden["particles_128x25"]["sha256"].items()})
     with open(os.path.join(HERE, "grid_golden.json"), "w") as fh:
         json.dump(golden, fh, indent=1, sort_keys=True)
         fh.write("\n")
