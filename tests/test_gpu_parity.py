@@ -302,3 +302,47 @@ def test_init_from_host_heightmap_is_a_fresh_world():
         assert np.array_equal(used.download(f), fresh.download(f)), f
     import ctypes
     assert H.lib.hg_init_heightmap_host(used.h, ctypes.c_void_p(0)) == -1  # HG_ERR_INVALID
+
+
+@pytest.mark.parametrize("p", [0.0, 1.0])
+@pytest.mark.parametrize("mode", [H.MODE_PLAIN, H.MODE_FUSED])
+def test_rain_probability_extremes(p, mode):
+    """Bernoulli rain at p = 0 (no cell ever rains) and p = 1 (the threshold
+    clamps to 2^32 - 1, so a cell whose word is all ones stays dry): the
+    GPU's rain and the steps after it equal the oracle bit for bit."""
+    w, ow, s, o = make_pair(128, "config2", p=p)
+    for k in range(12):
+        w.step(1, mode)
+        ow.step(s, o, 1)
+    assert_bitwise(w, ow, ctx=f"p={p}")
+    water = w.download("water")
+    assert (water.max() == 0.0) if p == 0.0 else (water.min() > 0.0)
+
+
+@pytest.mark.parametrize("hi,kspeed,tan", [(1e14, 0.3, 0.65), (1e-14, 0.3, 1e-14), (64.0, 50.0, 0.01)])
+@pytest.mark.parametrize("mode", [H.MODE_PLAIN, H.MODE_FUSED])
+def test_talus_extremes_bitwise_vs_oracle(hi, kspeed, tan, mode):
+    """Talus slippage far outside the workloads' range: heights up to 1e14
+    (marked-drop sums past 2^40, beyond the fused kernel's shared-reciprocal
+    range, so its IEEE division fallback runs), heights below 1e-14 with a
+    talus tangent of 1e-14 (sums below 2^-30, outflow scales below 2^-50:
+    the fallback again), and a slippage so fast that the outflows exceed the
+    material available (the shader's overshoot)."""
+    import math
+    n = 128
+    w = H.World(n)
+    w.init_heightmap(H.noise(seed=2, lo=0.0, hi=hi))
+    H.configure(w, "config2")
+    s = H.settings_config2()
+    s.Kspeed[0] = kspeed
+    s.Kalpha[0] = math.atan(tan)
+    w.set_erosion(s)
+    _, o = O.workload("config2")
+    ow = O.OracleWorld(n, 32)
+    ow.set("rock", w.download("rock"))
+    os_ = O.erosion_from(s)
+    for k in range(6):
+        w.step(1, mode)
+        ow.step(os_, o, 1)
+        assert_bitwise(w, ow, ctx=f"hi={hi} Kspeed={kspeed} step {k + 1}")
+    assert np.all(np.isfinite(w.download("rock")))
