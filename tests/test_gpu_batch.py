@@ -128,3 +128,38 @@ def test_batch_rejects_unfusable_world():
     with pytest.raises(H.HydrogenError) as e:
         b.step(1, H.MODE_FUSED)
     assert e.value.code == -5
+
+
+def test_largest_batch_in_one_launch():
+    """128 worlds (the most a batch holds; a 129th is refused) of 64² with
+    their own settings and seeds: one table launch per kernel for all of them,
+    the terrain lookup spanning its whole table, over 17 steps (two eight-step
+    graph replays and a direct step), equals each world's per-pass steps."""
+    ts = H.config3_terrains(count=129, seed=11)
+    for t in ts:
+        t["n"] = 64
+
+    def worlds(k):
+        out = []
+        for i, t in enumerate(ts[:k]):
+            w = H.make_config3_world(t, terrain_id=i)
+            w.set_options(H.options(H.RAIN_BERNOULLI, p=0.05, seed=t["seed"], terrain_id=i, tile=(64, 16), graph=1))
+            out.append(w)
+        return out
+    ref = worlds(128)
+    for w in ref:
+        w.step(17, H.MODE_PLAIN)
+    ws = worlds(128)
+    b = H.Batch(ws)
+    b.step(17, H.MODE_FUSED)
+    b.sync()
+    assert b.tuning()[0] == 0 and b.launch_form()[0] == 0  # the table launch ran
+    for a, c in zip(ref, ws):
+        same(a, c)
+    b.close()
+    extra = worlds(129)
+    with pytest.raises(H.HydrogenError) as e:
+        H.Batch(extra)
+    assert e.value.code == -5  # HG_ERR_UNSUPPORTED
+    for w in ref + ws + extra:
+        w.close()
