@@ -135,6 +135,7 @@ struct StepConsts {
     float Ks1;            // Ks[1]
     float Kconv;          // sediment conversion rock -> dirt
     float Kalpha1, Kspeed1;
+    int row_lo, row_hi;   // the per-pass kernels compute rows [row_lo, row_hi) only (a row slab)
 };
 
 // Layer 1's talus thresholds (as talus_x_cross, talus_b_diag, fast_div of

@@ -16,7 +16,7 @@ __device__ __forceinline__ size_t at(int n, int x, int y) { return (size_t)y * n
 __global__ void k_rain(StepConsts c, RainStep r, float* __restrict__ water) {
     int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x0 >= c.n || y >= c.n) return;
+    if (x0 >= c.n || y < c.row_lo || y >= c.row_hi) return;
     float4* p = reinterpret_cast<float4*>(water + at(c.n, x0, y));
     float4 d = *p;
     uint32_t w[4] = {0, 0, 0, 0};
@@ -38,7 +38,7 @@ __global__ void k_flux(StepConsts c, const float* __restrict__ rock, const float
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = c.n;
-    if (x >= n || y >= n) return;
+    if (x >= n || y < c.row_lo || y >= c.row_hi) return;
     size_t i = at(n, x, y);
     auto total = [&](int xx, int yy) -> float {
         if (xx < 0 || xx >= n || yy < 0 || yy >= n) return FAR_HEIGHT;
@@ -65,7 +65,7 @@ __global__ void k_erosion(StepConsts c, const float* __restrict__ u, const float
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = c.n;
-    if (x >= n || y >= n) return;
+    if (x >= n || y < c.row_lo || y >= c.row_hi) return;
     size_t i = at(n, x, y);
     float br = x < n - 1 ? rock[i + 1] : 0.0f;
     float bl = x > 0 ? rock[i - 1] : 0.0f;
@@ -85,7 +85,7 @@ __global__ void k_sediment(StepConsts c, const float* __restrict__ u, const floa
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = c.n;
-    if (x >= n || y >= n) return;
+    if (x >= n || y < c.row_lo || y >= c.row_hi) return;
     size_t i = at(n, x, y);
     float px, py;
     backtrace(c, x, y, u[i], v[i], px, py);
@@ -106,7 +106,7 @@ __global__ void k_thermal_out(StepConsts c, const float* __restrict__ rock, floa
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = c.n;
-    if (x >= n || y >= n) return;
+    if (x >= n || y < c.row_lo || y >= c.row_hi) return;
     size_t i = at(n, x, y);
     float b = rock[i];
     float nb[8];
@@ -129,7 +129,7 @@ __global__ void k_thermal_in(StepConsts c, const float* __restrict__ rock, const
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = c.n;
-    if (x >= n || y >= n) return;
+    if (x >= n || y < c.row_lo || y >= c.row_hi) return;
     size_t i = at(n, x, y);
     auto ok = [&](int xx, int yy) { return xx >= 0 && xx < n && yy >= 0 && yy < n; };
     float in[8];
@@ -151,7 +151,7 @@ __global__ void k_smooth(StepConsts c, const float* __restrict__ rock, float* __
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int n = c.n;
-    if (x >= n || y >= n) return;
+    if (x >= n || y < c.row_lo || y >= c.row_hi) return;
     size_t i = at(n, x, y);
     if (x == 0 || y == 0 || x == n - 1 || y == n - 1) {  // border texels are copied (:27-33)
         rock_o[i] = rock[i];

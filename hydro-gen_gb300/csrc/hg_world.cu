@@ -88,6 +88,7 @@ using namespace hg;
 
 struct hg_world {
     int n = 0;
+    int row_lo = 0, row_hi = 0;  // rows the per-pass kernels compute (hg_set_rows; all by default)
     int layers = 1;
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -316,6 +317,9 @@ bool thermal_on(const hg_world* w) {
 }
 
 StepConsts make_consts(const hg_world* w);
+// hg_set_rows restricted the per-pass kernels to a row slab: only one-layer
+// per-pass steps and single passes honour it
+bool rows_restricted(const hg_world* w) { return w->row_lo != 0 || w->row_hi != w->n; }
 // the reversed step covers rain, flux, erosion and sediment transport
 bool adjoint_covers(const hg_world* w) {
     return w->layers == 1 && make_consts(w).smooth_m == 0.0f && w->opt.rain_mode != HG_RAIN_REFERENCE;
@@ -326,6 +330,8 @@ StepConsts make_consts(const hg_world* w) {
     const hg_erosion_settings& s = w->es;
     volatile float dt = s.d_t;  // products rounded once, as the shaders do per cell
     c.n = w->n;
+    c.row_lo = w->row_lo;
+    c.row_hi = w->row_hi;
     c.dt = s.d_t;
     c.G = s.G;
     c.EK = s.ENERGY_KEPT;
@@ -785,6 +791,7 @@ int hg_world_create(int n, int layers, hg_world** out) {
     hg_world* w = new (std::nothrow) hg_world();
     if (!w) return fail(HG_ERR_OOM, "host allocation failed");
     w->n = n;
+    w->row_hi = n;
     w->layers = layers;
     cudaGetDevice(&w->device);
     hg_default_erosion_settings(&w->es);
@@ -1411,6 +1418,8 @@ int hg_step(hg_world* w, int nsteps, int mode) {
     if (nsteps < 0) return fail(HG_ERR_INVALID, "nsteps must be >= 0");
     if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_PARTICLES)
         return fail(HG_ERR_INVALID, "bad mode");
+    if (rows_restricted(w) && (mode != HG_MODE_PLAIN || w->layers != 1))
+        return fail(HG_ERR_UNSUPPORTED, "a row-restricted world steps with the one-layer per-pass kernels only");
     DeviceGuard g(w->device);
     StepConsts c = make_consts(w);
     cudaStream_t st = w->stream;
@@ -1537,6 +1546,91 @@ int hg_step(hg_world* w, int nsteps, int mode) {
     return HG_OK;
 }
 
+int hg_set_rows(hg_world* w, int lo, int hi) {
+    HG_CHECK_WORLD(w);
+    if (hi < 0) hi = w->n;
+    if (lo < 0 || lo > hi || hi > w->n) return fail(HG_ERR_INVALID, "rows must satisfy 0 <= lo <= hi <= n");
+    w->row_lo = lo;
+    w->row_hi = hi;
+    return HG_OK;
+}
+
+int hg_pass(hg_world* w, int pass, int layer) {
+    Range nv_range("hg_pass");
+    HG_CHECK_WORLD(w);
+    HG_CHECK_VALID(w);
+    if (w->layers != 1) return fail(HG_ERR_UNSUPPORTED, "single passes cover one-layer worlds");
+    if (pass < HG_PASS_RAIN || pass > HG_PASS_SMOOTHING) return fail(HG_ERR_INVALID, "bad pass");
+    if (layer != 0 && layer != 1) return fail(HG_ERR_INVALID, "layer must be 0 or 1");
+    DeviceGuard g(w->device);
+    const StepConsts c = make_consts(w);
+    cudaStream_t st = w->stream;
+    auto swap = [&](int f) { float* t = w->cur[f]; w->cur[f] = w->alt[f]; w->alt[f] = t; };
+    // the operations and buffer swaps of the one-layer per-pass step
+    switch (pass) {
+        case HG_PASS_RAIN:
+            rain_pass(w, c, w->step + 1, w->cur[S_ROCK], nullptr, w->cur[S_WATER], st);
+            break;
+        case HG_PASS_FLUX:
+            launch_flux(c, w->cur[S_ROCK], w->cur[S_WATER], w->cur[S_FL], w->cur[S_FR], w->cur[S_FT], w->cur[S_FB],
+                        w->alt[S_WATER], w->alt[S_FL], w->alt[S_FR], w->alt[S_FT], w->alt[S_FB], w->u, w->v, w->vz,
+                        st);
+            swap(S_WATER); swap(S_FL); swap(S_FR); swap(S_FT); swap(S_FB);
+            break;
+        case HG_PASS_EROSION:
+            launch_erosion(c, w->u, w->v, w->vz, w->cur[S_ROCK], w->alt[S_ROCK], w->cur[S_SED], st);
+            swap(S_ROCK);
+            break;
+        case HG_PASS_SEDIMENT:
+            launch_sediment(c, w->u, w->v, w->cur[S_SED], w->alt[S_SED], w->cur[S_WATER], st);
+            swap(S_SED);
+            break;
+        case HG_PASS_THERMAL_FLUX:  // the empty dirt layer's talus pass moves nothing
+            if (layer == 0) launch_thermal_out(c, w->cur[S_ROCK], w->tc, w->td, st);
+            break;
+        case HG_PASS_THERMAL_TRANSPORT:
+            if (layer == 0) {
+                launch_thermal_in(c, w->cur[S_ROCK], w->tc, w->td, w->alt[S_ROCK], st);
+                swap(S_ROCK);
+            }
+            break;
+        default:  // HG_PASS_SMOOTHING: the identity when Kspeed[1] == 0
+            if (c.smooth_m != 0.0f) {
+                launch_smooth(c, w->cur[S_ROCK], w->alt[S_ROCK], st);
+                swap(S_ROCK);
+            }
+            break;
+    }
+    w->dev_step_valid = false;
+    HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+
+int hg_world_rows(hg_world* w, int field, int y0, int y1, float* host, int write) {
+    HG_CHECK_WORLD(w);
+    if (!host) return fail(HG_ERR_INVALID, "null host pointer");
+    if (y0 < 0 || y0 > y1 || y1 > w->n) return fail(HG_ERR_INVALID, "rows must satisfy 0 <= y0 <= y1 <= n");
+    float* d = nullptr;
+    size_t per_cell = 1;
+    if (field == HG_ROWS_THERMAL_C || field == HG_ROWS_THERMAL_D) {
+        d = reinterpret_cast<float*>(field == HG_ROWS_THERMAL_C ? w->tc : w->td);
+        per_cell = 4;
+    } else {
+        d = field_ptr(w, field);
+    }
+    if (!d) return fail(HG_ERR_INVALID, "bad field id");
+    DeviceGuard g(w->device);
+    const size_t off = (size_t)y0 * w->n * per_cell, count = (size_t)(y1 - y0) * w->n * per_cell;
+    if (count) {
+        if (write)
+            HG_CUDA(cudaMemcpyAsync(d + off, host, count * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+        else
+            HG_CUDA(cudaMemcpyAsync(host, d + off, count * sizeof(float), cudaMemcpyDeviceToHost, w->stream));
+    }
+    HG_CUDA(cudaStreamSynchronize(w->stream));
+    return HG_OK;
+}
+
 int hg_world_tuning(const hg_world* w, int* tile_y, int* graph, double ms[4]) {
     HG_CHECK_WORLD(w);
     if (tile_y) *tile_y = w->tuning.th;
@@ -1598,7 +1692,10 @@ int hg_batch_step(hg_batch* b, int nsteps, int mode) {
     if (mode != HG_MODE_PLAIN && mode != HG_MODE_FUSED && mode != HG_MODE_FUSED_PER_WORLD)
         return fail(HG_ERR_INVALID, "bad mode");
     if (nsteps == 0) return HG_OK;
-    for (hg_world* w : b->worlds) HG_CHECK_VALID(w);
+    for (hg_world* w : b->worlds) {
+        HG_CHECK_VALID(w);
+        if (rows_restricted(w)) return fail(HG_ERR_UNSUPPORTED, "a batch steps whole worlds (hg_set_rows is set)");
+    }
     DeviceGuard g(b->device);
     bool two_layer = false;  // the table launch covers one-layer worlds
     for (hg_world* w : b->worlds) two_layer = two_layer || w->layers == 2;
@@ -1955,6 +2052,7 @@ int hg_forward(hg_tape* t) {
     hg_world* w = t->w;
     HG_CHECK_VALID(w);
     if (!adjoint_covers(w)) return fail(HG_ERR_UNSUPPORTED, "the adjoint covers one-layer worlds without smoothing (Kspeed[1] == 0) or the reference rain");
+    if (rows_restricted(w)) return fail(HG_ERR_UNSUPPORTED, "a tape steps the whole world (hg_set_rows is set)");
     DeviceGuard g(w->device);
     t->step0 = w->step;
     const size_t c = cells(w);

@@ -33,6 +33,10 @@ FIELDS = {"rock": 0, "water": 1, "sediment": 2, "flux_l": 3, "flux_r": 4, "flux_
           "vel_u": 7, "vel_v": 8, "vel_z": 9, "ks": 10, "dirt": 11, "sediment_dirt": 12,
           "momentum_x": 13, "momentum_y": 14}
 STATE_FIELDS = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux_b", "vel_u", "vel_v"]
+# single passes of the per-pass step (hg_pass) and the talus outflow planes' row ids (hg_world_rows)
+PASSES = {"rain": 0, "flux": 1, "erosion": 2, "sediment": 3, "thermal_flux": 4, "thermal_transport": 5,
+          "smoothing": 6}
+ROWS_THERMAL = {"thermal_c": 100, "thermal_d": 101}
 
 
 class Camera(ctypes.Structure):
@@ -131,6 +135,9 @@ def _load():
         "hg_world_get_step": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64)]),
         "hg_world_set_step": (ctypes.c_int, [P, ctypes.c_uint64]),
         "hg_step": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "hg_set_rows": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "hg_pass": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
+        "hg_world_rows": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]),
         "hg_sync": (ctypes.c_int, [P]),
         "hg_world_totals": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double)]),
         "hg_field_totals_noalloc": (ctypes.c_int, [ctypes.POINTER(P), ctypes.c_int, ctypes.c_size_t, P, P]),
@@ -419,6 +426,30 @@ class World:
 
     def download_device(self, field, ptr):
         check(lib.hg_world_download_device(self.h, FIELDS[field], ctypes.c_void_p(ptr)))
+
+    def restrict_rows(self, lo=0, hi=-1):
+        """Per-pass kernels compute rows [lo, hi) only (hi = -1: all rows)."""
+        check(lib.hg_set_rows(self.h, lo, hi))
+
+    def run_pass(self, name, layer=0):
+        """One pass of the one-layer per-pass step (PASSES)."""
+        check(lib.hg_pass(self.h, PASSES[name], layer))
+
+    def get_rows(self, field, y0, y1):
+        """Rows [y0, y1) of a field as float32 (rows, n), or (rows, n, 4) for
+        the talus outflow planes."""
+        fid = ROWS_THERMAL.get(field, None)
+        shape = (y1 - y0, self.n) if fid is None else (y1 - y0, self.n, 4)
+        a = np.empty(shape, np.float32)
+        check(lib.hg_world_rows(self.h, FIELDS[field] if fid is None else fid, y0, y1, a.ctypes.data, 0))
+        return a
+
+    def put_rows(self, field, y0, rows):
+        fid = ROWS_THERMAL.get(field, None)
+        a = np.ascontiguousarray(rows, dtype=np.float32)
+        y1 = y0 + a.shape[0]
+        assert a.size == (y1 - y0) * self.n * (1 if fid is None else 4)
+        check(lib.hg_world_rows(self.h, FIELDS[field] if fid is None else fid, y0, y1, a.ctypes.data, 1))
 
     def state(self, fields=STATE_FIELDS):
         return {f: self.download(f) for f in fields}

@@ -32,14 +32,19 @@ back-trace reach over the rows it computes (all-reduce); above the budget,
 every rank restores its rows from the block's start and steps the block
 with the per-pass schedule instead.
 
-This module is the host-side schedule only.  It drives any `stepper` that
-runs one pass over a row range and reads and writes rows of a field
-(`run_pass`, `set_compute_rows`, `get_rows`, `set_rows`, `max_reach_rows`,
-`set_step`), through torch.distributed collectives on CPU tensors (gloo; a
-GPU stepper would pass device tensors to NCCL).  The tests drive it with the
-float oracle's passes restricted to rows, bit for bit against one process
-stepping the whole world (tests/test_slabs_gloo.py).
+The schedule drives any `stepper` that runs one pass over a row range and
+reads and writes rows of a field (`run_pass`, `set_compute_rows`,
+`get_rows`, `set_rows`, `max_reach_rows`, `set_step`) through a `comm` that
+moves row blocks between ranks: `SlabComm` (torch.distributed, ranks as
+processes; gloo on CPU, NCCL between GPUs) or `ThreadComm` (ranks as threads
+of one process, rows through host memory).  `GpuSlabStepper` steps a rank's
+rows with the library's per-pass kernels (hg_set_rows, hg_pass,
+hg_world_rows).  The tests drive the schedule with the float oracle's passes
+on gloo ranks (tests/test_slabs_gloo.py) and with GPU steppers on threads
+(tests/test_gpu_slabs.py), bit for bit against one world stepped whole.
 """
+import threading
+
 import numpy as np
 
 # (pass, layer, [(field, halo rows or "reach"), ...]) in the step's order
@@ -220,3 +225,113 @@ def deep_block(stepper, comm, step1, nsteps, settings, rain_period, sed_budget=2
     stepper.set_compute_rows(lo, hi)
     comm.deep_blocks += 1
     return len(plans)
+
+
+class GpuSlabStepper:
+    """A rank's rows stepped by the library's one-layer per-pass kernels: a
+    world the size of the whole grid whose passes compute only the rows the
+    schedule names.  Fields travel as row blocks of four channels per cell,
+    packed as height (rock, water), flux (L, R, T, B), vel (u, v, depth),
+    sed (sediment) and the two talus outflow planes."""
+    PACK = {"height": ("rock", "water"), "flux": ("flux_l", "flux_r", "flux_t", "flux_b"),
+            "vel": ("vel_u", "vel_v", "vel_z"), "sed": ("sediment",)}
+    PLANES = {"thc": "thermal_c", "thd": "thermal_d"}
+
+    def __init__(self, world, rows, rank, dt):
+        self.w = world
+        self.lo, self.hi = rows[rank]
+        self.dt = dt
+
+    def run_pass(self, name, layer):
+        self.w.run_pass(name, layer)
+
+    def set_compute_rows(self, a, b):
+        self.w.restrict_rows(a, b)
+
+    def set_step(self, done):
+        self.w.step_count = done
+
+    def get_rows(self, tex, y0, y1):
+        out = np.zeros((y1 - y0, self.w.n, 4))
+        if tex in self.PLANES:
+            out[:] = self.w.get_rows(self.PLANES[tex], y0, y1)
+        else:
+            for k, f in enumerate(self.PACK[tex]):
+                out[..., k] = self.w.get_rows(f, y0, y1)
+        return out
+
+    def set_rows(self, tex, y0, rows):
+        if tex in self.PLANES:
+            self.w.put_rows(self.PLANES[tex], y0, rows)
+        else:
+            for k, f in enumerate(self.PACK[tex]):
+                self.w.put_rows(f, y0, rows[..., k])
+
+    def max_reach_rows(self, y0=None, y1=None):
+        y0 = self.lo if y0 is None else y0
+        y1 = self.hi if y1 is None else y1
+        v = self.w.get_rows("vel_v", y0, y1)
+        return int(np.ceil(np.max(np.abs(v)) * self.dt)) + 1 if v.size else 0
+
+
+class ThreadGroup:
+    """The ranks of one slab decomposition as threads of one process (one
+    GPU each, or several on one GPU): a barrier and a mailbox.  A rank that
+    fails calls abort(), and the others' next wait raises instead of
+    hanging; every wait also gives up after `timeout` seconds."""
+
+    def __init__(self, nranks, timeout=300.0):
+        self.nranks = nranks
+        self.timeout = timeout
+        self.barrier = threading.Barrier(nranks)
+        self.box = {}
+
+    def abort(self):
+        self.barrier.abort()
+
+
+class ThreadComm:
+    """SlabComm's operations between the threads of a ThreadGroup: halo rows
+    from the two neighbours, the all-gather and the maximum, through host
+    memory."""
+
+    def __init__(self, group, rank, rows, n):
+        self.g = group
+        self.rank, self.nranks, self.rows, self.n = rank, group.nranks, rows, n
+        self.min_rows = min(hi - lo for lo, hi in rows)
+        self.gathers = 0
+        self.exchanges = 0
+        self.deep_blocks = 0
+        self.rollbacks = 0
+
+    def _sync(self):
+        self.g.barrier.wait(self.g.timeout)
+
+    def agree_max(self, value):
+        self.g.box[("max", self.rank)] = float(value)
+        self._sync()
+        m = max(self.g.box[("max", r)] for r in range(self.nranks))
+        self._sync()  # every rank has read before the box is reused
+        return m
+
+    def exchange(self, stepper, field, depth):
+        lo, hi = self.rows[self.rank]
+        self.g.box[("lo", self.rank)] = stepper.get_rows(field, lo, lo + depth)
+        self.g.box[("hi", self.rank)] = stepper.get_rows(field, hi - depth, hi)
+        self._sync()
+        if self.rank > 0:
+            stepper.set_rows(field, lo - depth, self.g.box[("hi", self.rank - 1)])
+        if self.rank < self.nranks - 1:
+            stepper.set_rows(field, hi, self.g.box[("lo", self.rank + 1)])
+        self._sync()
+        self.exchanges += 1
+
+    def gather(self, stepper, field):
+        lo, hi = self.rows[self.rank]
+        self.g.box[("all", self.rank)] = stepper.get_rows(field, lo, hi)
+        self._sync()
+        for r, (a, b) in enumerate(self.rows):
+            if r != self.rank:
+                stepper.set_rows(field, a, self.g.box[("all", r)])
+        self._sync()
+        self.gathers += 1

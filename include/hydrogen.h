@@ -333,6 +333,37 @@ int hg_world_set_step(hg_world* w, uint64_t step);
  * thermal_erosion/thermal_transport.  mode selects the per-pass kernels or
  * the fused kernel; both give bit-identical fields.  Asynchronous. */
 int hg_step(hg_world* w, int nsteps, int mode);
+
+/* ---- row slabs (one grid over several GPUs) ------------------------------------------- */
+/* No counterpart in the reference, which dispatches every pass over the whole
+ * grid (src/erosion.cpp:92-101).  A rank that owns rows of a grid split into
+ * row slabs steps them with these, exchanging halo rows between passes (the
+ * schedule is hydrogen's slabs.py; its ranks may be processes or threads).
+ * hg_set_rows restricts the per-pass kernels to rows [lo, hi) (hi = -1: all
+ * rows, the default); while it is set, only one-layer per-pass steps and
+ * single passes run (fused steps, batches and tapes are refused with
+ * HG_ERR_UNSUPPORTED).  Rows outside the range keep whatever the buffer
+ * swaps leave there.  hg_pass runs one pass of the one-layer per-pass step,
+ * with that step's operations and buffer swaps: rain uses step number
+ * hg_world_get_step + 1 (set it with hg_world_set_step); the talus passes of
+ * layer 1 and smoothing with Kspeed[1] == 0 are identities; the reference's
+ * rain ignores the row range.  Asynchronous.  hg_world_rows copies rows
+ * [y0, y1) of a field between the world and caller-owned host memory (write
+ * != 0: into the world), n floats a row, or 4 n for the talus outflow planes
+ * (HG_ROWS_THERMAL_C: toward L, R, T, B; HG_ROWS_THERMAL_D: toward LT, RT,
+ * LB, RB).  Synchronous with respect to the host. */
+#define HG_PASS_RAIN 0
+#define HG_PASS_FLUX 1
+#define HG_PASS_EROSION 2
+#define HG_PASS_SEDIMENT 3
+#define HG_PASS_THERMAL_FLUX 4
+#define HG_PASS_THERMAL_TRANSPORT 5
+#define HG_PASS_SMOOTHING 6
+#define HG_ROWS_THERMAL_C 100
+#define HG_ROWS_THERMAL_D 101
+int hg_set_rows(hg_world* w, int lo, int hi);
+int hg_pass(hg_world* w, int pass, int layer);
+int hg_world_rows(hg_world* w, int field, int y0, int y1, float* host, int write);
 /* Replaces Erosion::dispatch_grid_rain (src/erosion.cpp:76-89) for callers
  * that keep the reference's own cadence (src/main.cpp:315-319): one rain
  * pass now, whatever the rain period, with the world's rain model

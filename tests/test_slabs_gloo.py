@@ -165,3 +165,48 @@ def test_deep_halo_blocks_equal_one_world(nranks, films):
         assert rollbacks > 0 and gathers > 0
     else:  # uniform rain: every block completed after its one exchange
         assert deep_blocks > 0 and rollbacks == 0 and gathers == 0
+
+
+@pytest.mark.parametrize("nranks,deep", [(2, 0), (3, 4)])
+def test_thread_ranks_equal_one_world(nranks, deep):
+    """The same schedules with the ranks as threads of one process
+    (slabs.ThreadComm: rows through host memory), thin films included: bit
+    for bit one world."""
+    import threading
+    sys.path.insert(0, os.path.join(ROOT, "hydro-gen_gb300"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import slabs
+    films = True
+    rows = slabs.slab_rows(N, nranks)
+    s, o = workload(O, films)
+    group = slabs.ThreadGroup(nranks, timeout=120.0)
+    out, errors = [None] * nranks, []
+
+    def rank_main(r):
+        try:
+            st = OracleSlab(O, rows, r, s, o, s.d_t)
+            comm = slabs.ThreadComm(group, r, rows, N)
+            k = 0
+            while k < STEPS:
+                if deep:
+                    k += slabs.deep_block(st, comm, k + 1, min(deep, STEPS - k), s, o.rain_period, sed_budget=3)
+                else:
+                    slabs.slab_step(st, comm, k + 1, s, o.rain_period, halo_max=8)
+                    k += 1
+            lo, hi = rows[r]
+            out[r] = {f: st.w.get(f)[lo:hi] for f in FIELDS}
+        except BaseException as e:  # let the other ranks' waits end
+            errors.append(e)
+            group.abort()
+
+    threads = [threading.Thread(target=rank_main, args=(r,)) for r in range(nranks)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    w = one_world(films)
+    for r, (lo, hi) in enumerate(rows):
+        for f in FIELDS:
+            assert np.array_equal(out[r][f], w.get(f)[lo:hi]), (r, f)
