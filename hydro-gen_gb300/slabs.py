@@ -99,7 +99,8 @@ def passes_of_step(step1, settings, rain_period, rain_on=True):
 
 class SlabComm:
     """Halo exchange and gather of row blocks between the ranks of a slab
-    decomposition (torch.distributed, any backend)."""
+    decomposition (torch.distributed: buffers on the current GPU under NCCL,
+    in host memory under gloo)."""
 
     def __init__(self, dist, rank, nranks, rows, n, channels=4):
         import torch
@@ -107,13 +108,16 @@ class SlabComm:
         self.dist = dist
         self.rank, self.nranks, self.rows, self.n, self.ch = rank, nranks, rows, n, channels
         self.min_rows = min(hi - lo for lo, hi in rows)
+        # NCCL moves device buffers, gloo host ones
+        nccl = dist.is_initialized() and dist.get_backend() == "nccl"
+        self.dev = torch.device("cuda", torch.cuda.current_device()) if nccl else torch.device("cpu")
         self.gathers = 0
         self.exchanges = 0
         self.deep_blocks = 0  # blocks of steps after one exchange
         self.rollbacks = 0    # blocks redone pass by pass (a back-trace beyond the budget)
 
     def agree_max(self, value):
-        t = self.torch.tensor([float(value)], dtype=self.torch.float64)
+        t = self.torch.tensor([float(value)], dtype=self.torch.float64, device=self.dev)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
         return float(t.item())
 
@@ -127,14 +131,14 @@ class SlabComm:
         for nb, send_rows, recv_at in ((self.rank - 1, (lo, lo + depth), lo - depth),
                                        (self.rank + 1, (hi - depth, hi), hi)):
             if 0 <= nb < self.nranks:
-                out = torch.from_numpy(np.ascontiguousarray(stepper.get_rows(field, *send_rows)))
+                out = torch.from_numpy(np.ascontiguousarray(stepper.get_rows(field, *send_rows))).to(self.dev)
                 inc = torch.empty_like(out)
                 reqs += [dist.isend(out, nb), dist.irecv(inc, nb)]
                 recv.append((recv_at, inc))
         for r in reqs:
             r.wait()
         for at, inc in recv:
-            stepper.set_rows(field, at, inc.numpy())
+            stepper.set_rows(field, at, inc.cpu().numpy())
         self.exchanges += 1
 
     def gather(self, stepper, field):
@@ -144,12 +148,12 @@ class SlabComm:
         h = max(b - a for a, b in self.rows)
         blk = np.zeros((h, self.n, self.ch))
         blk[: hi - lo] = stepper.get_rows(field, lo, hi)
-        mine = torch.from_numpy(blk)
+        mine = torch.from_numpy(blk).to(self.dev)
         allb = [torch.empty_like(mine) for _ in range(self.nranks)]
         self.dist.all_gather(allb, mine)
         for r, (a, b) in enumerate(self.rows):
             if r != self.rank:
-                stepper.set_rows(field, a, allb[r][: b - a].numpy())
+                stepper.set_rows(field, a, allb[r][: b - a].cpu().numpy())
         self.gathers += 1
 
 
