@@ -210,3 +210,50 @@ def test_thread_ranks_equal_one_world(nranks, deep):
     for r, (lo, hi) in enumerate(rows):
         for f in FIELDS:
             assert np.array_equal(out[r][f], w.get(f)[lo:hi]), (r, f)
+
+
+def test_thread_rank_failure_ends_the_others_waits():
+    """A rank that raises in the middle of a step (here: its stepper fails on
+    the third flux pass) aborts the group; the other rank's next wait raises
+    BrokenBarrierError at once instead of waiting out the timeout."""
+    import threading
+    import time
+    sys.path.insert(0, os.path.join(ROOT, "hydro-gen_gb300"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import slabs
+    rows = slabs.slab_rows(N, 2)
+    s, o = workload(O, False)
+    group = slabs.ThreadGroup(2, timeout=60.0)
+    seen = [None, None]
+
+    class Failing(OracleSlab):
+        flux_passes = 0
+
+        def run_pass(self, name, layer):
+            if name == "flux":
+                self.flux_passes += 1
+                if self.flux_passes == 3:
+                    raise RuntimeError("planted failure")
+            super().run_pass(name, layer)
+
+    def rank_main(r):
+        st = (Failing if r == 1 else OracleSlab)(O, rows, r, s, o, s.d_t)
+        comm = slabs.ThreadComm(group, r, rows, N)
+        try:
+            for k in range(STEPS):
+                slabs.slab_step(st, comm, k + 1, s, o.rain_period, halo_max=8)
+        except BaseException as e:
+            seen[r] = e
+            group.abort()
+
+    t0 = time.perf_counter()
+    threads = [threading.Thread(target=rank_main, args=(r,)) for r in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=120)
+    assert not any(t.is_alive() for t in threads)
+    assert isinstance(seen[1], RuntimeError)
+    assert isinstance(seen[0], threading.BrokenBarrierError)
+    assert time.perf_counter() - t0 < 30.0  # well inside the 60 s timeout
