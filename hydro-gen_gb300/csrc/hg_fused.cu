@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro(const __grid_constant__ 
 // parameter.  SPLIT as for hydro_block: the host picks it by world size.
 template <int TH, bool SPLIT>
 __global__ void __launch_bounds__(Geo<TH>::NTH) k_hydro1(const __grid_constant__ TerrainDesc td, int* err) {
-    hydro_block<TH, SPLIT>(td.h, td.maps, blockIdx.x, err);
+    hydro_block<TH, SPLIT>(td.h, td.maps, blockIdx.x + td.tile_off, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -531,7 +531,8 @@ __device__ __forceinline__ void transport_tile(const TerrainHot& td, const CUten
 }
 
 template <int TH, bool SPLIT>
-__device__ __forceinline__ void transport_block(const TerrainHot& td, const CUtensorMap* maps, int tile, int* err) {
+__device__ __forceinline__ void transport_block(const TerrainHot& td, const CUtensorMap* maps, int tile, int first_tile,
+                                                int* err) {
     using G = Geo<TH>;
     __shared__ __align__(128) float be[G::T_BOX];
     __shared__ __align__(16) float outf[8 * G::O_C];
@@ -547,19 +548,19 @@ __device__ __forceinline__ void transport_block(const TerrainHot& td, const CUte
     else transport_tile<TH, 1>(td, maps, be, outf, &bar, tx0, ty0, true, err);
     // k_hydro of this step has finished (stream order) and the next step's
     // k_hydro starts after this launch: advance the terrain's step counter
-    if (tile == 0 && threadIdx.x == 0) *td.step += 1ull;
+    if (tile == first_tile && threadIdx.x == 0) *td.step += 1ull;
 }
 
 template <int TH>
 __global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport(const __grid_constant__ BatchParams bp,
                                                             const CUtensorMap* __restrict__ maps, int* err) {
     const int t = find_terrain(bp.tile0, bp.nterr, blockIdx.x);
-    transport_block<TH, false>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], err);
+    transport_block<TH, false>(bp.t[t], maps + MAPS_PER_TERRAIN * t, blockIdx.x - bp.tile0[t], 0, err);
 }
 
 template <int TH, bool SPLIT>
 __global__ void __launch_bounds__(Geo<TH>::NTH, TH == 16 ? 4 : 6) k_transport1(const __grid_constant__ TerrainDesc td, int* err) {
-    transport_block<TH, SPLIT>(td.h, td.maps, blockIdx.x, err);
+    transport_block<TH, SPLIT>(td.h, td.maps, blockIdx.x + td.tile_off, td.tile_off, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -619,6 +620,7 @@ bool fill_desc(TerrainDesc& d, const TerrainSrc& s, int th, int tile0, TmaCache&
     h.step = s.step;
     h.tiles_x = s.c.n / TW;
     h.tile0 = tile0;
+    d.tile_off = 0;
     const int in_fields[H_N] = {S_ROCK, S_WATER, S_SED, S_FL, S_FR, S_FT, S_FB};
     for (int f = 0; f < H_N; ++f)
         if (!cache.get(s.in[in_fields[f]], s.c.n, th + 2, &d.maps[f])) return false;
@@ -646,6 +648,30 @@ template <int TH, bool SPLIT>
 void launch_one(const TerrainDesc& td, int tiles, int* err, cudaStream_t st) {
     k_hydro1<TH, SPLIT><<<tiles, Geo<TH>::NTH, 0, st>>>(td, err);
     k_transport1<TH, SPLIT><<<tiles, Geo<TH>::NTH, 0, st>>>(td, err);
+}
+
+// One kernel of the fused step (which 0: k_hydro, 1: k_transport) over the
+// `tiles` tiles from tile_lo on (whole tile rows: a row slab's).
+template <int TH, bool SPLIT>
+void launch_half(const TerrainDesc& td, int which, int tiles, int* err, cudaStream_t st) {
+    if (which == 0) k_hydro1<TH, SPLIT><<<tiles, Geo<TH>::NTH, 0, st>>>(td, err);
+    else k_transport1<TH, SPLIT><<<tiles, Geo<TH>::NTH, 0, st>>>(td, err);
+}
+
+void launch_fused_half(const TerrainDesc& td0, int th, int which, int tile_lo, int tiles, int* err,
+                       cudaStream_t st) {
+    if (tiles <= 0) return;
+    TerrainDesc td = td0;
+    td.tile_off = tile_lo;
+    const bool split = td.h.c.n >= SPLIT_MIN_N;
+    if (th == 16) {
+        if (split) launch_half<16, true>(td, which, tiles, err, st);
+        else launch_half<16, false>(td, which, tiles, err, st);
+    } else {
+        if (split) launch_half<8, true>(td, which, tiles, err, st);
+        else launch_half<8, false>(td, which, tiles, err, st);
+    }
+    count_launch();
 }
 
 void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st) {

@@ -168,6 +168,7 @@ constexpr int MAPS_PER_TERRAIN = 8;
 struct TerrainDesc {
     CUtensorMap maps[MAPS_PER_TERRAIN];
     TerrainHot h;
+    int tile_off;  // first tile launched (a row slab's), 0 for the whole world
 };
 // A batch launch's terrain records travel as one kernel parameter (read
 // through the constant bank); the tensor maps stay in global memory.
@@ -214,6 +215,9 @@ void launch_fused_table(const BatchParams& bp, const CUtensorMap* maps, int tota
                         cudaStream_t st);
 // Same for one terrain whose descriptor travels as a kernel parameter.
 void launch_fused_one(const TerrainDesc& td, int th, int* err, cudaStream_t st);
+// One kernel of the fused step (which 0: k_hydro, 1: k_transport) over tiles
+// [tile_lo, tile_lo + tiles) of a single world.
+void launch_fused_half(const TerrainDesc& td, int th, int which, int tile_lo, int tiles, int* err, cudaStream_t st);
 
 // ---- adjoint (hg_adjoint.cu) ----------------------------------------------------------
 // A step's state or its adjoint: rock, water, sediment, fL, fR, fT, fB.

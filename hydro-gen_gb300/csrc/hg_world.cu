@@ -1606,6 +1606,50 @@ int hg_pass(hg_world* w, int pass, int layer) {
     return HG_OK;
 }
 
+int hg_fused_pass(hg_world* w, int which) {
+    Range nv_range("hg_fused_pass");
+    HG_CHECK_WORLD(w);
+    HG_CHECK_VALID(w);
+    if (which != 0 && which != 1) return fail(HG_ERR_INVALID, "which must be 0 (k_hydro) or 1 (k_transport)");
+    if (w->layers != 1) return fail(HG_ERR_UNSUPPORTED, "fused halves cover one-layer worlds");
+    const int th = 16;
+    if (!fused_tile_ok(w->n, th)) return fail(HG_ERR_UNSUPPORTED, "fused mode needs n divisible by 64");
+    const StepConsts c = make_consts(w);
+    if (c.smooth_m != 0.0f || w->opt.rain_mode == HG_RAIN_REFERENCE)
+        return fail(HG_ERR_UNSUPPORTED, "fused halves cover worlds without smoothing or the reference rain");
+    if (w->row_lo % th || w->row_hi % th)
+        return fail(HG_ERR_INVALID, "fused halves step whole tile rows: the row range must be multiples of 16");
+    DeviceGuard g(w->device);
+    cudaStream_t st = w->stream;
+    if (!w->dev_step_valid) {
+        k_set_u64<<<1, 1, 0, st>>>(w->d_step, (unsigned long long)w->step);
+        w->dev_step_valid = true;
+    }
+    TerrainSrc src{};
+    src.c = c;
+    src.rain = make_rain_base(w);
+    src.step = w->d_step;
+    for (int f = 0; f < S_COUNT; ++f) {
+        src.in[f] = w->cur[f];
+        src.out[f] = w->alt[f];
+    }
+    src.u = w->u;
+    src.v = w->v;
+    src.s_ero = w->s_ero;
+    src.b_ero = w->b_ero;
+    TerrainDesc td;
+    if (!fill_desc(td, src, th, 0, w->tma)) return fail(HG_ERR_CUDA, "cuTensorMapEncodeTiled failed for a world buffer");
+    const int tiles_x = w->n / 64;
+    launch_fused_half(td, th, which, (w->row_lo / th) * tiles_x, ((w->row_hi - w->row_lo) / th) * tiles_x, w->err,
+                      st);
+    if (which == 1) {  // the step's outputs become the state (k_transport advanced the device counter)
+        for (int f = 0; f < S_COUNT; ++f) std::swap(w->cur[f], w->alt[f]);
+        w->step += 1;
+    }
+    HG_CUDA(cudaGetLastError());
+    return HG_OK;
+}
+
 int hg_world_rows(hg_world* w, int field, int y0, int y1, float* host, int write) {
     HG_CHECK_WORLD(w);
     if (!host) return fail(HG_ERR_INVALID, "null host pointer");
@@ -1615,6 +1659,8 @@ int hg_world_rows(hg_world* w, int field, int y0, int y1, float* host, int write
     if (field == HG_ROWS_THERMAL_C || field == HG_ROWS_THERMAL_D) {
         d = reinterpret_cast<float*>(field == HG_ROWS_THERMAL_C ? w->tc : w->td);
         per_cell = 4;
+    } else if (field == HG_ROWS_ERODED_ROCK || field == HG_ROWS_ERODED_SEDIMENT) {
+        d = field == HG_ROWS_ERODED_ROCK ? w->b_ero : w->s_ero;
     } else {
         d = field_ptr(w, field);
     }

@@ -36,7 +36,8 @@ STATE_FIELDS = ["rock", "water", "sediment", "flux_l", "flux_r", "flux_t", "flux
 # single passes of the per-pass step (hg_pass) and the talus outflow planes' row ids (hg_world_rows)
 PASSES = {"rain": 0, "flux": 1, "erosion": 2, "sediment": 3, "thermal_flux": 4, "thermal_transport": 5,
           "smoothing": 6}
-ROWS_THERMAL = {"thermal_c": 100, "thermal_d": 101}
+# row-transfer ids beyond FIELDS: (id, floats per cell)
+ROWS_EXTRA = {"thermal_c": (100, 4), "thermal_d": (101, 4), "eroded_rock": (102, 1), "eroded_sediment": (103, 1)}
 
 
 class Camera(ctypes.Structure):
@@ -138,6 +139,7 @@ def _load():
         "hg_set_rows": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
         "hg_pass": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int]),
         "hg_world_rows": (ctypes.c_int, [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]),
+        "hg_fused_pass": (ctypes.c_int, [P, ctypes.c_int]),
         "hg_sync": (ctypes.c_int, [P]),
         "hg_world_totals": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double)]),
         "hg_field_totals_noalloc": (ctypes.c_int, [ctypes.POINTER(P), ctypes.c_int, ctypes.c_size_t, P, P]),
@@ -435,21 +437,25 @@ class World:
         """One pass of the one-layer per-pass step (PASSES)."""
         check(lib.hg_pass(self.h, PASSES[name], layer))
 
+    def fused_pass(self, which):
+        """One kernel of the fused step over the restricted rows (0: k_hydro,
+        1: k_transport, after which the step is done)."""
+        check(lib.hg_fused_pass(self.h, which))
+
     def get_rows(self, field, y0, y1):
         """Rows [y0, y1) of a field as float32 (rows, n), or (rows, n, 4) for
         the talus outflow planes."""
-        fid = ROWS_THERMAL.get(field, None)
-        shape = (y1 - y0, self.n) if fid is None else (y1 - y0, self.n, 4)
-        a = np.empty(shape, np.float32)
-        check(lib.hg_world_rows(self.h, FIELDS[field] if fid is None else fid, y0, y1, a.ctypes.data, 0))
+        fid, per = ROWS_EXTRA.get(field, (FIELDS.get(field), 1))
+        a = np.empty((y1 - y0, self.n) if per == 1 else (y1 - y0, self.n, per), np.float32)
+        check(lib.hg_world_rows(self.h, fid, y0, y1, a.ctypes.data, 0))
         return a
 
     def put_rows(self, field, y0, rows):
-        fid = ROWS_THERMAL.get(field, None)
+        fid, per = ROWS_EXTRA.get(field, (FIELDS.get(field), 1))
         a = np.ascontiguousarray(rows, dtype=np.float32)
         y1 = y0 + a.shape[0]
-        assert a.size == (y1 - y0) * self.n * (1 if fid is None else 4)
-        check(lib.hg_world_rows(self.h, FIELDS[field] if fid is None else fid, y0, y1, a.ctypes.data, 1))
+        assert a.size == (y1 - y0) * self.n * per
+        check(lib.hg_world_rows(self.h, fid, y0, y1, a.ctypes.data, 1))
 
     def state(self, fields=STATE_FIELDS):
         return {f: self.download(f) for f in fields}

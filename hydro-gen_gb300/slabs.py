@@ -176,6 +176,28 @@ def slab_step(stepper, comm, step1, settings, rain_period, halo_max=8, rain_on=T
         stepper.run_pass(name, layer)
 
 
+def fused_slab_step(stepper, comm, thermal=True, halo_max=8):
+    """One step of the owned rows with the two fused kernels (whole tile rows:
+    slabs of multiples of 16 rows; no smoothing).  k_hydro reads its tile's
+    total height and flux one row around; k_transport reads the eroded rock
+    two rows around (the talus passes, when on) and the eroded sediment at
+    the back-traces (an exchange as deep as they reach, else the all-gather)."""
+    lo, hi = comm.rows[comm.rank]
+    stepper.set_compute_rows(lo, hi)
+    comm.exchange(stepper, "height", 1)
+    comm.exchange(stepper, "flux", 1)
+    stepper.fused_half(0)
+    if thermal:
+        comm.exchange(stepper, "ero_rock", 2)
+    reach = int(comm.agree_max(stepper.max_reach_rows()))
+    if reach <= min(halo_max, comm.min_rows):
+        if reach > 0:
+            comm.exchange(stepper, "ero_sed", reach)
+    else:
+        comm.gather(stepper, "ero_sed")
+    stepper.fused_half(1)
+
+
 def block_depth(plans, sed_budget):
     """Halo rows a block of steps needs: the read radii of its passes."""
     return sum(sed_budget if name == "sediment" else PASS_RADIUS[name] for plan in plans for name, _, _ in plan)
@@ -238,7 +260,8 @@ class GpuSlabStepper:
     packed as height (rock, water), flux (L, R, T, B), vel (u, v, depth),
     sed (sediment) and the two talus outflow planes."""
     PACK = {"height": ("rock", "water"), "flux": ("flux_l", "flux_r", "flux_t", "flux_b"),
-            "vel": ("vel_u", "vel_v", "vel_z"), "sed": ("sediment",)}
+            "vel": ("vel_u", "vel_v", "vel_z"), "sed": ("sediment",),
+            "ero_rock": ("eroded_rock",), "ero_sed": ("eroded_sediment",)}
     PLANES = {"thc": "thermal_c", "thd": "thermal_d"}
 
     def __init__(self, world, rows, rank, dt):
@@ -248,6 +271,9 @@ class GpuSlabStepper:
 
     def run_pass(self, name, layer):
         self.w.run_pass(name, layer)
+
+    def fused_half(self, which):
+        self.w.fused_pass(which)
 
     def set_compute_rows(self, a, b):
         self.w.restrict_rows(a, b)

@@ -361,9 +361,21 @@ int hg_step(hg_world* w, int nsteps, int mode);
 #define HG_PASS_SMOOTHING 6
 #define HG_ROWS_THERMAL_C 100
 #define HG_ROWS_THERMAL_D 101
+#define HG_ROWS_ERODED_ROCK 102      /* the fused step's hand-off between its two kernels */
+#define HG_ROWS_ERODED_SEDIMENT 103
 int hg_set_rows(hg_world* w, int lo, int hi);
 int hg_pass(hg_world* w, int pass, int layer);
 int hg_world_rows(hg_world* w, int field, int y0, int y1, float* host, int write);
+/* One kernel of the fused step over the restricted rows (which 0: rain, flux,
+ * erosion, writing the eroded rock and sediment; 1: sediment gather and talus
+ * passes, then the step's outputs become the state and the step counter
+ * advances).  Between the two, the rows that k_transport reads around a
+ * rank's own come from its neighbours: the eroded rock two rows deep and the
+ * eroded sediment as deep as the back-traces reach (HG_ROWS_ERODED_*).  For
+ * one-layer worlds of sides divisible by 64 without smoothing or the
+ * reference's rain; the row range must be whole tile rows (multiples of
+ * 16).  Asynchronous. */
+int hg_fused_pass(hg_world* w, int which);
 /* Replaces Erosion::dispatch_grid_rain (src/erosion.cpp:76-89) for callers
  * that keep the reference's own cadence (src/main.cpp:315-319): one rain
  * pass now, whatever the rain period, with the world's rain model

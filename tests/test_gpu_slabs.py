@@ -113,3 +113,66 @@ def test_row_restricted_world_refuses_whole_world_paths():
     w.restrict_rows()
     w.step(1, H.MODE_FUSED)
     w.close()
+
+
+def make_fused(films, n=128):
+    """Config-2 physics (talus slippage, no smoothing) for the fused halves."""
+    w = H.World(n)
+    w.init_heightmap(H.noise(seed=1, frequency=1.0 / 16))
+    H.configure(w, "config2")
+    if films:
+        w.set_options(H.options(H.RAIN_BERNOULLI, p=0.05, seed=3))
+    else:
+        w.set_rain(H.rain_uniform(0.01, 1))
+        w.set_options(H.options(H.RAIN_UNIFORM))
+    return w
+
+
+@pytest.mark.parametrize("nranks,films", [(2, False), (2, True), (4, True)])
+def test_gpu_fused_slabs_equal_one_world(nranks, films):
+    """The fused step on row slabs (hg_fused_pass; slabs.fused_slab_step):
+    k_hydro on each rank's tile rows after a one-row exchange of height and
+    flux, the eroded rock two rows deep and the eroded sediment as deep as
+    the back-traces reach (or the all-gather) between the kernels, then
+    k_transport; every rank's rows equal one world stepped with the fused
+    kernels, bit for bit."""
+    n = 128
+    rows = slabs.slab_rows(n, nranks)
+    group = slabs.ThreadGroup(nranks, timeout=120.0)
+    worlds = [make_fused(films, n) for _ in range(nranks)]
+    dt = H.settings_config2().d_t
+    out, errors = [None] * nranks, []
+
+    def rank_main(r):
+        try:
+            st = slabs.GpuSlabStepper(worlds[r], rows, r, dt)
+            comm = slabs.ThreadComm(group, r, rows, n)
+            for _ in range(STEPS):
+                slabs.fused_slab_step(st, comm, thermal=True, halo_max=8)
+            worlds[r].sync()
+            lo, hi = rows[r]
+            out[r] = ({f: worlds[r].get_rows(f, lo, hi) for f in FIELDS}, (comm.exchanges, comm.gathers))
+        except BaseException as e:  # let the other ranks' waits end
+            errors.append(e)
+            group.abort()
+
+    threads = [threading.Thread(target=rank_main, args=(r,)) for r in range(nranks)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    ref = make_fused(films, n)
+    ref.step(STEPS, H.MODE_FUSED)
+    gathers = 0
+    for r, (lo, hi) in enumerate(rows):
+        fields, (ex, ga) = out[r]
+        gathers += ga
+        assert worlds[r].step_count == STEPS
+        for f in FIELDS:
+            g = ref.download(f)[lo:hi]
+            bad = np.argwhere(fields[f].view(np.uint32) != g.view(np.uint32))
+            assert bad.size == 0, f"rank {r} {f}: {len(bad)} cells differ, first {bad[:3].tolist()}"
+    assert (gathers > 0) == films
+    for w in worlds:
+        w.close()
