@@ -39,8 +39,10 @@ moves row blocks between ranks: `SlabComm` (torch.distributed, ranks as
 processes; gloo on CPU, NCCL between GPUs) or `ThreadComm` (ranks as threads
 of one process, rows through host memory).  `GpuSlabStepper` steps a rank's
 rows with the library's per-pass kernels (hg_set_rows, hg_pass,
-hg_world_rows).  The tests drive the schedule with the float oracle's passes
-on gloo ranks (tests/test_slabs_gloo.py) and with GPU steppers on threads
+hg_world_rows); `fused_slab_step` steps them with its two fused kernels
+instead (hg_fused_pass), exchanging the hand-off between them.  The tests
+drive the schedules with the float oracle's passes on gloo ranks and on
+threads (tests/test_slabs_gloo.py) and with GPU steppers on threads
 (tests/test_gpu_slabs.py), bit for bit against one world stepped whole.
 """
 import threading
