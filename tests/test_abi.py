@@ -73,6 +73,11 @@ def test_error_paths_without_a_device(hg):
     assert (fs.nsteps, fs.ckpt_every, fs.iters) == (256, 32, 8)
     assert hg.lib.hg_inverse_fit(None, None, None, None, ctypes.byref(fs), None, None) == -1
     assert hg.lib.hg_init_heightmap_host(None, None) == -1
+    # the row-slab entry points refuse a null world before any CUDA call
+    assert hg.lib.hg_set_rows(None, 0, 8) == -1
+    assert hg.lib.hg_pass(None, 1, 0) == -1
+    assert hg.lib.hg_fused_pass(None, 0) == -1
+    assert hg.lib.hg_world_rows(None, 0, 0, 1, None, 0) == -1
     # the allocation-free totals check their arguments before any CUDA call
     out = ctypes.c_void_p(1)
     ptrs = (ctypes.c_void_p * 9)(*([1] * 9))
