@@ -257,3 +257,65 @@ def test_thread_rank_failure_ends_the_others_waits():
     assert isinstance(seen[1], RuntimeError)
     assert isinstance(seen[0], threading.BrokenBarrierError)
     assert time.perf_counter() - t0 < 30.0  # well inside the 60 s timeout
+
+
+@pytest.mark.parametrize("reach,expect", [(2, "exchange"), (50, "gather")])
+def test_fused_slab_step_schedule(reach, expect):
+    """slabs.fused_slab_step on two thread ranks with a stepper that records
+    what it is asked: the rank's rows, a one-row exchange of height and flux,
+    k_hydro, the eroded rock two rows deep, the agreed back-trace reach, the
+    eroded sediment that deep (or the all-gather past the halo limit), then
+    k_transport."""
+    import threading
+    sys.path.insert(0, os.path.join(ROOT, "hydro-gen_gb300"))
+    import slabs
+    n = 64
+    rows = slabs.slab_rows(n, 2)
+    group = slabs.ThreadGroup(2, timeout=60.0)
+    logs, errors = [[], []], []
+
+    class Recorder:
+        def __init__(self, r):
+            self.r = r
+
+        def set_compute_rows(self, a, b):
+            logs[self.r].append(("rows", a, b))
+
+        def get_rows(self, tex, y0, y1):
+            logs[self.r].append(("get", tex, y1 - y0))
+            return np.zeros((y1 - y0, n, 4))
+
+        def set_rows(self, tex, y0, data):
+            logs[self.r].append(("set", tex, data.shape[0]))
+
+        def fused_half(self, which):
+            logs[self.r].append(("half", which))
+
+        def max_reach_rows(self):
+            return reach if self.r == 1 else 1
+
+    def rank_main(r):
+        try:
+            slabs.fused_slab_step(Recorder(r), slabs.ThreadComm(group, r, rows, n), thermal=True, halo_max=8)
+        except BaseException as e:
+            errors.append(e)
+            group.abort()
+
+    threads = [threading.Thread(target=rank_main, args=(r,)) for r in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=60)
+    assert not errors, errors
+    for r in range(2):
+        ev = logs[r]
+        assert ev[0] == ("rows",) + rows[r]
+        halves = [i for i, e in enumerate(ev) if e[0] == "half"]
+        assert [ev[i][1] for i in halves] == [0, 1]
+        before, between = ev[:halves[0]], ev[halves[0] + 1:halves[1]]
+        assert ("set", "height", 1) in before and ("set", "flux", 1) in before
+        assert ("set", "ero_rock", 2) in between
+        if expect == "exchange":  # the agreed reach (the larger rank's) deep
+            assert ("set", "ero_sed", reach) in between
+        else:  # past the halo limit: every other rank's rows
+            assert ("set", "ero_sed", rows[1 - r][1] - rows[1 - r][0]) in between
